@@ -1,0 +1,148 @@
+/*
+ * nufft3d.h -- C ABI of libnufft3d.so, the sm_103a (GB300) implementation of
+ * the @nufft_3d hot path of marcsous/nufft_3d: Kaiser-Bessel interpolation
+ * set-up, forward fNUFT, adjoint aNUFT, density compensation and the iNUFT
+ * iterative reconstruction.
+ *
+ * Every entry point replaces one piece of the reference's MATLAB interface
+ * (file:line relative to the reference project root).  The layouts are the
+ * reference's: column-major MATLAB arrays, complex values interleaved
+ * (re, im) as MATLAB's interleaved complex API stores them.
+ *
+ *   om   [3 x M]            double, cycles/FOV (nufft_3d.m:11)
+ *   x    [N1 N2 N3 nc]      complex single image
+ *   k    [M nc]             complex single samples
+ *   W, d [M]                real single weights
+ *
+ * Pointers named *_dev are device pointers on the plan's device; *_host are
+ * host pointers (pinned memory gives the fastest copies).  `stream` is a
+ * cudaStream_t passed as void* (NULL = the legacy default stream).  All calls
+ * return NUFFT3D_SUCCESS (0) or a negative status; nufft3d_last_error()
+ * returns a thread-local message for the last failure on the calling thread.
+ *
+ * A plan is immutable after creation except for its internal scratch buffers:
+ * calls on the same plan must not overlap (serialise them on one stream, or
+ * create one plan per stream).  Plans on different devices or different plans
+ * on one device are independent.
+ */
+#ifndef NUFFT3D_H
+#define NUFFT3D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NUFFT3D_SUCCESS 0
+#define NUFFT3D_ERR_ARG (-1)          /* invalid argument (reference error() conditions) */
+#define NUFFT3D_ERR_SIZE (-2)         /* size mismatch or prod(K) >= 2^31 */
+#define NUFFT3D_ERR_CUDA (-3)         /* CUDA runtime failure */
+#define NUFFT3D_ERR_NOMEM (-4)        /* device or host allocation failed */
+#define NUFFT3D_ERR_UNSUPPORTED (-5)  /* option outside what this build implements */
+#define NUFFT3D_ERR_TIMEOUT (-6)      /* a bounded wait expired */
+
+#define NUFFT3D_SOLVER_MINRES 0       /* iNUFT.m:136 (reference default) */
+#define NUFFT3D_SOLVER_CG 1           /* conjugate gradients, FP64 scalars */
+
+typedef struct nufft3d_plan nufft3d_plan;
+
+/* Constructor options: the reference's name/value pairs (nufft_3d.m:26-43,
+ * 70-76) plus tuning knobs.  Fill with nufft3d_opts_default() first. */
+typedef struct nufft3d_opts {
+    double J;          /* kernel width ('J', default 4) */
+    double u;          /* oversampling ('u', default 2) */
+    double alpha;      /* Kaiser-Bessel alpha ('alpha', 0 = Beatty formula) */
+    int radial;        /* 1 = radial kernel, 0 = separable ('radial', default 1) */
+    int gpu;           /* 'gpu': 1 = single-precision GPU (the only path built);
+                          0 (CPU) and 2 (double GPU) return NUFFT3D_ERR_UNSUPPORTED */
+    int device;        /* CUDA device ordinal for the plan (default: current) */
+    const float *d;    /* 'd': optional host density [M] (NULL = density.m) */
+    int density_iters; /* density.m:5 maxit (default 20) */
+    int tile[3];       /* interpolation tile shape (0 = autotune/default) */
+    int max_coils_per_pass; /* coils handled per interpolation pass (0 = auto) */
+    int max_samples_per_block; /* samples per interpolation block (0 = auto) */
+    int verbose;       /* print the reference's set-up summary to stdout */
+} nufft3d_opts;
+
+/* Read-only properties (nufft_3d.m:26-43). */
+typedef struct nufft3d_info {
+    int32_t N[3];      /* image size (N3 = 1 in 2D, nufft_3d.m:104-106) */
+    int32_t K[3];      /* oversampled grid, K = 2*ceil(N*u/2) (nufft_3d.m:109) */
+    int64_t M;         /* number of samples (rows of H) */
+    int64_t nnz;       /* samples within bounds (nufft_3d.m:126) */
+    double J, u, alpha;
+    int radial;
+    int tile[3];       /* interpolation tile shape in use */
+    int64_t n_blocks;  /* interpolation blocks (tile pieces) */
+    double taps_per_sample; /* mean nonzeros per row of H */
+    int64_t device_bytes;   /* device memory held by the plan (tables + scratch) */
+} nufft3d_info;
+
+/* Fills *opts with the reference defaults: J=4, u=2, alpha=0 (Beatty),
+ * radial=1, gpu=1, density_iters=20 (nufft_3d.m:27-36, density.m:5). */
+int nufft3d_opts_default(nufft3d_opts *opts);
+
+/* obj = nufft_3d(om, N, name, value, ...)  -- nufft_3d.m:54-251.
+ * om_host: [3 x M] doubles (cycles/FOV).  N: 1 or 3 even integers
+ * (n_N = 1 or 3).  Builds the sorted interpolation plan, the deapodization U
+ * (deap.m) and, unless opts->d is given, the density d (density.m). */
+int nufft3d_plan_create(const double *om_host, int64_t M, const int32_t *N, int n_N,
+                        const nufft3d_opts *opts, nufft3d_plan **plan);
+
+int nufft3d_plan_destroy(nufft3d_plan *plan);
+
+int nufft3d_plan_info(const nufft3d_plan *plan, nufft3d_info *info);
+
+/* obj.U (deap.m:2-36,98): [N1 N2 N3] real single, copied to host. */
+int nufft3d_get_deap(const nufft3d_plan *plan, float *U_host);
+
+/* obj.d (density.m:2-42, or the user density, zero out of bounds): [M]. */
+int nufft3d_get_density(const nufft3d_plan *plan, float *d_host);
+
+/* k = obj.fNUFT(x)  -- fNUFT.m:2-9: k = H*fft3_pad(U.*x)/sqrt(nnz). */
+int nufft3d_forward(nufft3d_plan *plan, const float *x_dev, float *k_dev, int nc,
+                    void *stream);
+
+/* x = obj.aNUFT(k)  -- aNUFT.m:2-9: x = U.*ifft3_crop(H'*k)/sqrt(nnz). */
+int nufft3d_adjoint(nufft3d_plan *plan, const float *k_dev, float *x_dev, int nc,
+                    void *stream);
+
+/* y = iprojection(x, damp, W) -- nufft_3d.m:305-313:
+ * y = aNUFT(W.*fNUFT(x)) + damp^2*x.  W_dev: [M] or NULL for W = d. */
+int nufft3d_normal(nufft3d_plan *plan, const float *x_dev, float *y_dev, int nc,
+                   double damp, const float *W_dev, void *stream);
+
+/* Host-pointer variants of fNUFT / aNUFT: copy in, run, copy out, synchronise. */
+int nufft3d_forward_host(nufft3d_plan *plan, const float *x_host, float *k_host, int nc);
+int nufft3d_adjoint_host(nufft3d_plan *plan, const float *k_host, float *x_host, int nc);
+
+/* im = obj.iNUFT(raw, maxit, damp, W)  -- iNUFT.m:2-138,224-227 default path.
+ * raw_dev [M nc]; W_dev [M] sample weights multiplied by d (iNUFT.m:72), or
+ * NULL for W = d; maxit = 0 is regridding aNUFT(W.*raw) (iNUFT.m:119-122).
+ * Each coil is solved as its own system (A'WA + damp^2 I) x = A'W raw with
+ * x0 = 0; solver MINRES (reference) or CG; tol as iNUFT.m:114 (1e-4), tol = 0
+ * runs exactly maxit iterations.  iters_host (optional, [nc]) receives the
+ * iteration count per coil. */
+int nufft3d_inverse(nufft3d_plan *plan, const float *raw_dev, float *x_dev, int nc,
+                    int maxit, double damp, const float *W_dev, int solver, double tol,
+                    int *iters_host, void *stream);
+
+int nufft3d_inverse_host(nufft3d_plan *plan, const float *raw_host, float *x_host, int nc,
+                         int maxit, double damp, const float *W_host, int solver,
+                         double tol, int *iters_host);
+
+/* Re-runs density.m on the plan (maxit iterations) and stores it as obj.d. */
+int nufft3d_density(nufft3d_plan *plan, int maxit);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *nufft3d_last_error(void);
+
+/* Library version string. */
+const char *nufft3d_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NUFFT3D_H */

@@ -1,0 +1,423 @@
+// Oversampled 3-D FFT of fNUFT / aNUFT as three pruned line passes.
+//
+// Replaces fft3_pad / ifft3_crop of @nufft_3d/nufft_3d.m:285-302 (cuFFT via
+// gpuArray in the reference).  Per axis j the reference zero-pads (K-N)/2 on
+// both sides, fftshifts and takes a length-K FFT; the inverse takes an
+// unnormalised inverse FFT (ifft * K), ifftshifts and crops the central N.
+// Both shifts reduce to a slot map: image index n (0..N-1) <-> FFT slot
+// (n - N/2) mod K, so no padded array is ever materialised.
+//
+// Layouts (complex64, coil fastest inside the library):
+//   image  [nc][N3][N2][N1]   (MATLAB [N1 N2 N3 nc])
+//   B1     [N3][N2][K1][nc]   after the x pass
+//   B2     [N3][K2][K1][nc]   after the y pass
+//   G      [K3][K2][K1][nc]   oversampled grid
+// Forward: FX (image*U -> B1), FY (B1 -> B2), FZ (B2 -> G).
+// Adjoint: IZ (G -> B2), IY (B2 -> B1), IX (B1 -> image, *U*scale).
+//
+// Each block runs a mixed-radix Stockham FFT (radix 2,3,4,5,7,8,11,13) on a
+// batch of lines held in shared memory; the inverse is conj(FFT(conj(x))).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <vector>
+
+#include "internal.h"
+
+namespace nufft3d {
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// multiply by -i
+__device__ __forceinline__ float2 cmi(float2 a) { return make_float2(a.y, -a.x); }
+
+template <int R>
+__device__ __forceinline__ void dft(float2 (&u)[R], const float2 *__restrict__ tw, int n)
+{
+    // generic small prime: y_q = sum_t u_t W_R^{qt}, W from the length-n table
+    float2 y[R];
+    const int step = n / R;
+#pragma unroll
+    for (int q = 0; q < R; ++q) {
+        float2 acc = u[0];
+#pragma unroll
+        for (int t = 1; t < R; ++t) acc = cadd(acc, cmul(u[t], __ldg(&tw[((q * t) % R) * step])));
+        y[q] = acc;
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q) u[q] = y[q];
+}
+
+template <>
+__device__ __forceinline__ void dft<2>(float2 (&u)[2], const float2 *__restrict__, int)
+{
+    float2 a = u[0], b = u[1];
+    u[0] = cadd(a, b);
+    u[1] = csub(a, b);
+}
+
+template <>
+__device__ __forceinline__ void dft<3>(float2 (&u)[3], const float2 *__restrict__, int)
+{
+    const float s3 = 0.86602540378443864676f; // sin(2 pi / 3)
+    float2 t = cadd(u[1], u[2]);
+    float2 d = csub(u[1], u[2]);
+    float2 y0 = cadd(u[0], t);
+    float2 m = make_float2(u[0].x - 0.5f * t.x, u[0].y - 0.5f * t.y);
+    float2 s = make_float2(s3 * d.y, -s3 * d.x); // -i * s3 * d
+    u[0] = y0;
+    u[1] = cadd(m, s);
+    u[2] = csub(m, s);
+}
+
+template <>
+__device__ __forceinline__ void dft<4>(float2 (&u)[4], const float2 *__restrict__, int)
+{
+    float2 t0 = cadd(u[0], u[2]), t1 = csub(u[0], u[2]);
+    float2 t2 = cadd(u[1], u[3]), t3 = cmi(csub(u[1], u[3]));
+    u[0] = cadd(t0, t2);
+    u[2] = csub(t0, t2);
+    u[1] = cadd(t1, t3);
+    u[3] = csub(t1, t3);
+}
+
+template <>
+__device__ __forceinline__ void dft<5>(float2 (&u)[5], const float2 *__restrict__, int)
+{
+    const float c1 = 0.30901699437494742410f, c2 = -0.80901699437494742410f;
+    const float s1 = 0.95105651629515357212f, s2 = 0.58778525229247312917f;
+    float2 t1 = cadd(u[1], u[4]), t2 = cadd(u[2], u[3]);
+    float2 t3 = csub(u[1], u[4]), t4 = csub(u[2], u[3]);
+    float2 y0 = cadd(u[0], cadd(t1, t2));
+    float2 b1 = make_float2(u[0].x + c1 * t1.x + c2 * t2.x, u[0].y + c1 * t1.y + c2 * t2.y);
+    float2 b2 = make_float2(u[0].x + c2 * t1.x + c1 * t2.x, u[0].y + c2 * t1.y + c1 * t2.y);
+    float2 e1 = make_float2(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
+    float2 e2 = make_float2(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
+    float2 d1 = cmi(e1), d2 = cmi(e2);
+    u[0] = y0;
+    u[1] = cadd(b1, d1);
+    u[4] = csub(b1, d1);
+    u[2] = cadd(b2, d2);
+    u[3] = csub(b2, d2);
+}
+
+template <>
+__device__ __forceinline__ void dft<8>(float2 (&u)[8], const float2 *__restrict__ tw, int n)
+{
+    // radix-2 split: evens and odds through radix-4, combined with W8^k
+    float2 e[4] = {u[0], u[2], u[4], u[6]};
+    float2 o[4] = {u[1], u[3], u[5], u[7]};
+    dft<4>(e, tw, n);
+    dft<4>(o, tw, n);
+    const float h = 0.70710678118654752440f;
+    float2 o1 = make_float2(h * (o[1].x + o[1].y), h * (o[1].y - o[1].x)); // * (1-i)/sqrt2
+    float2 o2 = cmi(o[2]);                                                   // * -i
+    float2 o3 = make_float2(h * (o[3].y - o[3].x), -h * (o[3].x + o[3].y)); // * (-1-i)/sqrt2
+    u[0] = cadd(e[0], o[0]);
+    u[4] = csub(e[0], o[0]);
+    u[1] = cadd(e[1], o1);
+    u[5] = csub(e[1], o1);
+    u[2] = cadd(e[2], o2);
+    u[6] = csub(e[2], o2);
+    u[3] = cadd(e[3], o3);
+    u[7] = csub(e[3], o3);
+}
+
+// One Stockham stage: lines of length n, stride LS; p = product of the
+// radices already applied.  Output position j + q*p with j = (i-k)*R + k.
+template <int R>
+__device__ __forceinline__ void fft_stage(const float2 *__restrict__ a, float2 *__restrict__ b,
+                                          int nlines, int LS, int n, int p,
+                                          const float2 *__restrict__ tw)
+{
+    const int m = n / R;
+    const int total = nlines * m;
+    const int twstep = n / (p * R);
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int line = t / m;
+        const int i = t - line * m;
+        const int k = i % p;
+        const float2 *src = a + line * LS;
+        float2 *dst = b + line * LS;
+        float2 u[R];
+#pragma unroll
+        for (int q = 0; q < R; ++q) u[q] = src[i + q * m];
+        if (k) {
+#pragma unroll
+            for (int q = 1; q < R; ++q) u[q] = cmul(u[q], __ldg(&tw[q * k * twstep]));
+        }
+        dft<R>(u, tw, n);
+        const int j = (i - k) * R + k;
+#pragma unroll
+        for (int q = 0; q < R; ++q) dst[j + q * p] = u[q];
+    }
+}
+
+// Forward FFT of `nlines` lines held in a (stride LS); b is the ping-pong
+// buffer.  Returns the buffer holding the result.
+__device__ float2 *block_fft(float2 *a, float2 *b, int nlines, int LS, const FFTDesc &f)
+{
+    int p = 1;
+    for (int s = 0; s < f.nst; ++s) {
+        const int r = f.rad[s];
+        switch (r) {
+        case 2: fft_stage<2>(a, b, nlines, LS, f.n, p, f.tw); break;
+        case 3: fft_stage<3>(a, b, nlines, LS, f.n, p, f.tw); break;
+        case 4: fft_stage<4>(a, b, nlines, LS, f.n, p, f.tw); break;
+        case 5: fft_stage<5>(a, b, nlines, LS, f.n, p, f.tw); break;
+        case 7: fft_stage<7>(a, b, nlines, LS, f.n, p, f.tw); break;
+        case 8: fft_stage<8>(a, b, nlines, LS, f.n, p, f.tw); break;
+        case 11: fft_stage<11>(a, b, nlines, LS, f.n, p, f.tw); break;
+        case 13: fft_stage<13>(a, b, nlines, LS, f.n, p, f.tw); break;
+        default: break;
+        }
+        __syncthreads();
+        float2 *t = a;
+        a = b;
+        b = t;
+        p *= r;
+    }
+    return a;
+}
+
+__device__ __forceinline__ int slot_of(int n, int N, int K)
+{
+    int s = n - N / 2;
+    return s < 0 ? s + K : s;
+}
+
+// ------------------------------------------------------------- kernels
+constexpr int kFftThreads = 256;
+constexpr int kMaxLineCoils = 16;
+
+// FX: image (user layout) * U -> B1, length-K1 FFT along x for one (y,z) line
+// of up to kMaxLineCoils coils.  fNUFT.m:5 + nufft_3d.m:287-289 (j=1).
+__global__ void __launch_bounds__(kFftThreads)
+k_fx(const float2 *__restrict__ img, const float *__restrict__ U, float2 *__restrict__ B1,
+     int N1, int N23, int nc, FFTDesc fd)
+{
+    extern __shared__ float2 sm[];
+    const int K = fd.n, LS = K + 1;
+    const int line = blockIdx.x;
+    const int c0 = blockIdx.y * kMaxLineCoils;
+    const int nv = min(kMaxLineCoils, nc - c0);
+    float2 *A = sm, *B = sm + nv * LS;
+    const int nz = K - N1;
+    for (int t = threadIdx.x; t < nz * nv; t += blockDim.x) {
+        const int v = t / nz, j = t - v * nz;
+        A[v * LS + N1 / 2 + j] = make_float2(0.f, 0.f);
+    }
+    const float *Ur = U + (size_t)line * N1;
+    for (int t = threadIdx.x; t < N1 * nv; t += blockDim.x) {
+        const int v = t / N1, n = t - v * N1;
+        float2 val = img[((size_t)(c0 + v) * N23 + line) * N1 + n];
+        const float w = __ldg(&Ur[n]);
+        A[v * LS + slot_of(n, N1, K)] = make_float2(val.x * w, val.y * w);
+    }
+    __syncthreads();
+    const float2 *res = block_fft(A, B, nv, LS, fd);
+    float2 *ob = B1 + (size_t)line * K * nc + c0;
+    for (int t = threadIdx.x; t < K * nv; t += blockDim.x) {
+        const int k = t / nv, v = t - k * nv;
+        ob[(size_t)k * nc + v] = res[v * LS + k];
+    }
+}
+
+// IX: B1 -> image, unnormalised inverse FFT along x, crop, *U*scale
+// (+ add_coef * addend).  nufft_3d.m:296-298 (j=1) + aNUFT.m:8-9.
+__global__ void __launch_bounds__(kFftThreads)
+k_ix(const float2 *__restrict__ B1, const float *__restrict__ U, float2 *__restrict__ img,
+     int N1, int N23, int nc, FFTDesc fd, float scale, const float2 *__restrict__ addend,
+     float add_coef)
+{
+    extern __shared__ float2 sm[];
+    const int K = fd.n, LS = K + 1;
+    const int line = blockIdx.x;
+    const int c0 = blockIdx.y * kMaxLineCoils;
+    const int nv = min(kMaxLineCoils, nc - c0);
+    float2 *A = sm, *B = sm + nv * LS;
+    const float2 *ib = B1 + (size_t)line * K * nc + c0;
+    for (int t = threadIdx.x; t < K * nv; t += blockDim.x) {
+        const int k = t / nv, v = t - k * nv;
+        float2 val = ib[(size_t)k * nc + v];
+        A[v * LS + k] = make_float2(val.x, -val.y);
+    }
+    __syncthreads();
+    const float2 *res = block_fft(A, B, nv, LS, fd);
+    const float *Ur = U + (size_t)line * N1;
+    for (int t = threadIdx.x; t < N1 * nv; t += blockDim.x) {
+        const int v = t / N1, n = t - v * N1;
+        const float2 r = res[v * LS + slot_of(n, N1, K)];
+        const float w = __ldg(&Ur[n]) * scale;
+        const size_t idx = ((size_t)(c0 + v) * N23 + line) * N1 + n;
+        float2 o = make_float2(r.x * w, -r.y * w);
+        if (addend) {
+            const float2 a = addend[idx];
+            o.x = fmaf(add_coef, a.x, o.x);
+            o.y = fmaf(add_coef, a.y, o.y);
+        }
+        img[idx] = o;
+    }
+}
+
+// Strided pass along y or z over rows of contiguous complex vectors.
+__global__ void __launch_bounds__(kFftThreads)
+k_line(const float2 *__restrict__ in, float2 *__restrict__ out, LinePass lp, FFTDesc fd, int inv)
+{
+    extern __shared__ float2 sm[];
+    const int K = fd.n, LS = K + 1, vec = lp.vec;
+    float2 *A = sm, *B = sm + vec * LS;
+    const int outer = blockIdx.x / lp.nchunks;
+    const int chunk = blockIdx.x - outer * lp.nchunks;
+    const float2 *ib = in + outer * lp.in_outer_stride + (int64_t)chunk * vec;
+    float2 *ob = out + outer * lp.out_outer_stride + (int64_t)chunk * vec;
+    const float sg = inv ? -1.f : 1.f;
+    if (lp.pad_in) {
+        const int nz = K - lp.Nimg;
+        for (int t = threadIdx.x; t < nz * vec; t += blockDim.x) {
+            const int v = t / nz, j = t - v * nz;
+            A[v * LS + lp.Nimg / 2 + j] = make_float2(0.f, 0.f);
+        }
+    }
+    for (int t = threadIdx.x; t < lp.n_in * vec; t += blockDim.x) {
+        const int i = t / vec, v = t - i * vec;
+        const float2 val = ib[(int64_t)i * lp.in_axis_stride + v];
+        const int slot = lp.pad_in ? slot_of(i, lp.Nimg, K) : i;
+        A[v * LS + slot] = make_float2(val.x, sg * val.y);
+    }
+    __syncthreads();
+    const float2 *res = block_fft(A, B, vec, LS, fd);
+    for (int t = threadIdx.x; t < lp.n_out * vec; t += blockDim.x) {
+        const int o = t / vec, v = t - o * vec;
+        const int slot = lp.crop_out ? slot_of(o, lp.Nimg, K) : o;
+        const float2 r = res[v * LS + slot];
+        ob[(int64_t)o * lp.out_axis_stride + v] = make_float2(r.x, sg * r.y);
+    }
+}
+
+// ----------------------------------------------------------------- host
+bool fft_factor(int n, FFTDesc &d)
+{
+    d.n = n;
+    d.nst = 0;
+    int m = n;
+    const int order[] = {8, 4, 2, 3, 5, 7, 11, 13};
+    for (int r : order) {
+        while (m % r == 0 && d.nst < 16) {
+            // a lone factor 2 after 8s is fine; prefer 4 over 2*2
+            d.rad[d.nst++] = r;
+            m /= r;
+        }
+    }
+    return m == 1;
+}
+
+static int line_vec(int64_t rowlen)
+{
+    const int cands[] = {16, 8, 4, 2, 1};
+    for (int v : cands)
+        if (rowlen % v == 0) return v;
+    return 1;
+}
+
+static size_t line_smem(int vec, int K) { return (size_t)2 * vec * (K + 1) * sizeof(float2); }
+
+static int launch_line(const float2 *in, float2 *out, int n_outer, int64_t rowlen,
+                       int n_in, int n_out, int Nimg, int pad_in, int crop_out,
+                       int64_t in_axis, int64_t out_axis, int64_t in_outer, int64_t out_outer,
+                       const FFTDesc &fd, int inv, cudaStream_t s)
+{
+    LinePass lp;
+    lp.vec = line_vec(rowlen);
+    lp.nchunks = (int)(rowlen / lp.vec);
+    lp.n_in = n_in;
+    lp.n_out = n_out;
+    lp.Nimg = Nimg;
+    lp.pad_in = pad_in;
+    lp.crop_out = crop_out;
+    lp.in_axis_stride = in_axis;
+    lp.out_axis_stride = out_axis;
+    lp.in_outer_stride = in_outer;
+    lp.out_outer_stride = out_outer;
+    const int64_t nblk = (int64_t)n_outer * lp.nchunks;
+    if (nblk <= 0) return NUFFT3D_SUCCESS;
+    if (nblk > 0x7fffffff) return fail(NUFFT3D_ERR_SIZE, "FFT pass grid too large");
+    k_line<<<(unsigned)nblk, kFftThreads, line_smem(lp.vec, fd.n), s>>>(in, out, lp, fd, inv);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
+int launch_fx(nufft3d_plan *p, const float2 *img, float2 *B1, int nc, cudaStream_t s)
+{
+    const int N1 = p->N[0], N23 = p->N[1] * p->N[2];
+    const FFTDesc &fd = p->fft[0];
+    const int nv = nc < kMaxLineCoils ? nc : kMaxLineCoils;
+    dim3 grid(N23, (nc + kMaxLineCoils - 1) / kMaxLineCoils);
+    k_fx<<<grid, kFftThreads, line_smem(nv, fd.n), s>>>(img, p->U, B1, N1, N23, nc, fd);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
+int launch_ix(nufft3d_plan *p, const float2 *B1, float2 *img, int nc, float scale,
+              const float2 *addend, float add_coef, cudaStream_t s)
+{
+    const int N1 = p->N[0], N23 = p->N[1] * p->N[2];
+    const FFTDesc &fd = p->fft[0];
+    const int nv = nc < kMaxLineCoils ? nc : kMaxLineCoils;
+    dim3 grid(N23, (nc + kMaxLineCoils - 1) / kMaxLineCoils);
+    k_ix<<<grid, kFftThreads, line_smem(nv, fd.n), s>>>(B1, p->U, img, N1, N23, nc, fd, scale,
+                                                        addend, add_coef);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
+int launch_fy(nufft3d_plan *p, const float2 *B1, float2 *B2, int nc, cudaStream_t s)
+{
+    const int64_t K1 = p->geom.K[0], K2 = p->geom.K[1];
+    const int64_t N2 = p->N[1], N3 = p->N[2];
+    const int64_t row = K1 * nc;
+    return launch_line(B1, B2, (int)N3, row, (int)N2, (int)K2, (int)N2, 1, 0, row, row,
+                       N2 * row, K2 * row, p->fft[1], 0, s);
+}
+
+int launch_fz(nufft3d_plan *p, const float2 *B2, float2 *G, int nc, cudaStream_t s)
+{
+    const int64_t K1 = p->geom.K[0], K2 = p->geom.K[1], K3 = p->geom.K[2];
+    const int64_t N3 = p->N[2];
+    const int64_t row = K1 * nc;
+    return launch_line(B2, G, (int)K2, row, (int)N3, (int)K3, (int)N3, 1, 0, K2 * row, K2 * row,
+                       row, row, p->fft[2], 0, s);
+}
+
+int launch_iz(nufft3d_plan *p, const float2 *G, float2 *B2, int nc, cudaStream_t s)
+{
+    const int64_t K1 = p->geom.K[0], K2 = p->geom.K[1], K3 = p->geom.K[2];
+    const int64_t N3 = p->N[2];
+    const int64_t row = K1 * nc;
+    return launch_line(G, B2, (int)K2, row, (int)K3, (int)N3, (int)N3, 0, 1, K2 * row, K2 * row,
+                       row, row, p->fft[2], 1, s);
+}
+
+int launch_iy(nufft3d_plan *p, const float2 *B2, float2 *B1, int nc, cudaStream_t s)
+{
+    const int64_t K1 = p->geom.K[0], K2 = p->geom.K[1];
+    const int64_t N2 = p->N[1], N3 = p->N[2];
+    const int64_t row = K1 * nc;
+    return launch_line(B2, B1, (int)N3, row, (int)K2, (int)N2, (int)N2, 0, 1, row, row,
+                       K2 * row, N2 * row, p->fft[1], 1, s);
+}
+
+int configure_fft_kernels()
+{
+    const int max_smem = 227 * 1024;
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fx, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_ix, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    return NUFFT3D_SUCCESS;
+}
+
+} // namespace nufft3d

@@ -1,0 +1,201 @@
+// Internal declarations shared by the libnufft3d translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/nufft3d.h"
+
+namespace nufft3d {
+
+// ---------------------------------------------------------------- errors
+void set_error(const std::string &msg);
+void clear_error();
+int fail(int code, const std::string &msg);
+
+#define NUFFT_CUDA_TRY(expr)                                                        \
+    do {                                                                            \
+        cudaError_t e_ = (expr);                                                    \
+        if (e_ != cudaSuccess)                                                      \
+            return ::nufft3d::fail(NUFFT3D_ERR_CUDA, std::string(#expr) + ": " +    \
+                                   cudaGetErrorString(e_));                         \
+    } while (0)
+
+#define NUFFT_TRY(expr)                                                             \
+    do {                                                                            \
+        int s_ = (expr);                                                            \
+        if (s_ != NUFFT3D_SUCCESS) return s_;                                       \
+    } while (0)
+
+// ----------------------------------------------------------- KB kernel
+// Kaiser-Bessel kernel of kernel.m:2-11 evaluated in registers:
+//   w(d2) = I0(alpha*sqrt(1 - d2/(J/2)^2)) / I0(alpha)
+// with the Numerical Recipes I0 polynomial (kernel.m:14-30).  The large-
+// argument branch is rearranged as exp(ax - alpha) * rsqrt(ax) * poly *
+// (exp(alpha)/I0(alpha)) so no intermediate leaves single-precision range.
+struct KBParams {
+    float alpha;        // KB alpha
+    float inv_half2;    // 1/(J/2)^2
+    float a2_over;      // alpha^2 / 3.75^2 (small-branch test/argument)
+    float inv_i0a;      // 1/I0(alpha)
+    float exp_over_i0a; // exp(alpha)/I0(alpha)
+    float half2;        // (J/2)^2: tap kept iff dist2 <= half2 (4*dist2 <= J^2)
+};
+
+__device__ __forceinline__ float kb_weight(float dist2, const KBParams &p)
+{
+    float t = fmaxf(fmaf(-dist2, p.inv_half2, 1.0f), 0.0f);
+    float y = p.a2_over * t; // (ax/3.75)^2
+    if (y < 1.0f) {
+        float s = fmaf(y, 0.45813e-2f, 0.360768e-1f);
+        s = fmaf(y, s, 0.2659732f);
+        s = fmaf(y, s, 1.2067492f);
+        s = fmaf(y, s, 3.0899424f);
+        s = fmaf(y, s, 3.5156229f);
+        s = fmaf(y, s, 1.0f);
+        return s * p.inv_i0a;
+    }
+    float ax = p.alpha * sqrtf(t);
+    float z = 3.75f / ax;
+    float s = fmaf(z, 0.392377e-2f, -0.1647633e-1f);
+    s = fmaf(z, s, 0.2635537e-1f);
+    s = fmaf(z, s, -0.2057706e-1f);
+    s = fmaf(z, s, 0.916281e-2f);
+    s = fmaf(z, s, -0.157565e-2f);
+    s = fmaf(z, s, 0.225319e-2f);
+    s = fmaf(z, s, 0.1328592e-1f);
+    s = fmaf(z, s, 0.39894228f);
+    return expf(ax - p.alpha) * rsqrtf(ax) * s * p.exp_over_i0a;
+}
+
+// ------------------------------------------------------------ geometry
+struct Geom {
+    int K[3];
+    int T[3];     // tile shape
+    int P[3];     // padded tile = T + 2*Ra
+    int Ra[3];    // halo per axis (R, or 0 along z in 2D)
+    int nt[3];    // tiles per axis
+    int R;        // ceil(J/2)
+    int radial;
+    int is2d;
+};
+
+// ------------------------------------------------------------------ FFT
+struct FFTDesc {
+    int n;
+    int nst;
+    int rad[16];
+    const float2 *tw; // tw[j] = exp(-2 pi i j / n), j < n
+};
+
+bool fft_factor(int n, FFTDesc &d);
+
+// Strided line pass over rows of contiguous complex vectors (FY/FZ/IY/IZ).
+struct LinePass {
+    int n_in, n_out, Nimg, pad_in, crop_out, vec, nchunks;
+    int64_t in_axis_stride, out_axis_stride, in_outer_stride, out_outer_stride;
+};
+
+// ----------------------------------------------------------------- plan
+struct Scratch {
+    int nc = 0;
+    float2 *B1 = nullptr, *B2 = nullptr, *G = nullptr, *ks = nullptr;
+    size_t bytes = 0;
+};
+
+struct HostStage {
+    size_t bytes_in = 0, bytes_out = 0;
+    float *in = nullptr, *out = nullptr;   // device staging for host-pointer calls
+};
+
+struct SolverWork {
+    int nc = 0;
+    size_t nimg = 0;
+    float2 *x = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *v = nullptr,
+           *vprev = nullptr, *w1 = nullptr, *w2 = nullptr;
+    double *partial = nullptr;  // [nc * nchunk]
+    double *scal = nullptr;     // per-coil scalar state
+    int *iters = nullptr;       // per-coil iteration counts
+    int nchunk = 0;
+};
+
+} // namespace nufft3d
+
+struct nufft3d_plan {
+    int device = 0;
+    int N[3] = {0, 0, 0};
+    int64_t M = 0, nnz = 0;
+    double J = 4, u = 2, alpha = 0, i0a = 1;
+    int radial = 1;
+    nufft3d::Geom geom{};
+    nufft3d::KBParams kb{};
+    // sorted samples
+    float4 *samples = nullptr;  // (fx, fy, fz, packed local coords), sorted by tile
+    int32_t *perm = nullptr;    // sorted -> original
+    int32_t *inv = nullptr;     // original -> sorted, -1 out of bounds
+    int4 *blocks = nullptr;     // (tile, start, count, 0)
+    int64_t n_blocks = 0;
+    int coils_per_pass = 8;
+    int threads = 256;
+    double taps = 0;
+    float *U = nullptr;         // deapodization [N1 N2 N3]
+    float *d = nullptr;         // density, sorted order [nnz]
+    float *d_orig = nullptr;    // density, original order [M] (0 out of bounds)
+    float2 *tw[3] = {nullptr, nullptr, nullptr};
+    nufft3d::FFTDesc fft[3];
+    nufft3d::Scratch scratch;
+    nufft3d::HostStage stage;
+    nufft3d::SolverWork solver;
+    float *wbuf = nullptr;      // sorted sample weights for iNUFT (W.*d)
+    int64_t table_bytes = 0;
+    cudaStream_t own_stream = nullptr;
+};
+
+namespace nufft3d {
+
+// Launchers (stream-ordered, no synchronisation).
+int ensure_scratch(nufft3d_plan *p, int nc);
+int launch_fx(nufft3d_plan *p, const float2 *img, float2 *B1, int nc, cudaStream_t s);
+int launch_fy(nufft3d_plan *p, const float2 *B1, float2 *B2, int nc, cudaStream_t s);
+int launch_fz(nufft3d_plan *p, const float2 *B2, float2 *G, int nc, cudaStream_t s);
+int launch_iz(nufft3d_plan *p, const float2 *G, float2 *B2, int nc, cudaStream_t s);
+int launch_iy(nufft3d_plan *p, const float2 *B2, float2 *B1, int nc, cudaStream_t s);
+// IX: img = scale*U*ifft_x(B1) + add_coef*addend (addend may be null)
+int launch_ix(nufft3d_plan *p, const float2 *B1, float2 *img, int nc, float scale,
+              const float2 *addend, float add_coef, cudaStream_t s);
+
+// gather: ks[s*nc + c] = scale * w_s * sum_taps w * G[...]  (wsample may be null)
+int launch_gather(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, float scale,
+                  const float *wsample, cudaStream_t s);
+// spread: G += H' ks (G zeroed by caller)
+int launch_spread(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, cudaStream_t s);
+// user [M nc] <-> sorted [nnz][nc]
+int launch_permute_out(nufft3d_plan *p, const float2 *ks, float2 *k, int nc, float scale,
+                       cudaStream_t s);
+int launch_permute_in(nufft3d_plan *p, const float2 *k, float2 *ks, int nc,
+                      const float *wsorted, cudaStream_t s);
+
+// whole operators on the plan's scratch
+int op_forward(nufft3d_plan *p, const float2 *x, float2 *k, int nc, cudaStream_t s);
+int op_adjoint(nufft3d_plan *p, const float2 *k, float2 *x, int nc, cudaStream_t s);
+// y = A'WA x + damp^2 x, wsorted = W.*d in sorted order (null = d)
+int op_normal(nufft3d_plan *p, const float2 *x, float2 *y, int nc, double damp,
+              const float *wsorted, cudaStream_t s);
+
+int op_adjoint_weighted(nufft3d_plan *p, const float2 *k, float2 *x, int nc, const float *wsorted,
+                        cudaStream_t s);
+// iNUFT.m:72: W.*d in sorted order (d itself when W_orig is null)
+int prepare_weights(nufft3d_plan *p, const float *W_orig, const float **wsorted, cudaStream_t s);
+int refresh_density_orig(nufft3d_plan *p, cudaStream_t s);
+
+int run_density(nufft3d_plan *p, int maxit, cudaStream_t s);
+int run_inverse(nufft3d_plan *p, const float2 *raw, float2 *x, int nc, int maxit,
+                double damp, const float *W_orig, int solver, double tol, int *iters_host,
+                cudaStream_t s);
+
+size_t smem_interp_bytes(const Geom &g, int cb);
+int configure_kernels();
+
+} // namespace nufft3d

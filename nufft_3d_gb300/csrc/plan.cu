@@ -1,0 +1,682 @@
+// Plan construction: the @nufft_3d constructor (nufft_3d.m:54-251).
+//
+// Instead of assembling the sparse matrix H (nufft_3d.m:129-212, ~113
+// nonzeros per sample for J=6 radial), the plan keeps
+//   * the in-bounds samples sorted by oversampled-grid tile (a permutation),
+//     each as (frac offset, packed tile-local position);
+//   * the tile pieces ("blocks") of at most max_samples_per_block samples;
+//   * the deapodization U (deap.m) in FP32, built in FP64 on the host;
+//   * the density d (density.m) or the user's d;
+//   * FFT twiddle tables built in FP64.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include <cub/device/device_radix_sort.cuh>
+
+#include "internal.h"
+
+namespace nufft3d {
+
+// ------------------------------------------------------------- errors
+static thread_local std::string g_last_error;
+
+void set_error(const std::string &msg) { g_last_error = msg; }
+void clear_error() { g_last_error.clear(); }
+int fail(int code, const std::string &msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+// -------------------------------------------------- FP64 kernel (host)
+// kernel.m:14-34, real or complex argument (complex only for deap.m's
+// untruncated samples beyond J/2).
+static const double kSmall[7] = {1.0, 3.5156229, 3.0899424, 1.2067492, 0.2659732, 0.360768e-1,
+                                 0.45813e-2};
+static const double kLarge[9] = {0.39894228, 0.1328592e-1, 0.225319e-2, -0.157565e-2, 0.916281e-2,
+                                 -0.2057706e-1, 0.2635537e-1, -0.1647633e-1, 0.392377e-2};
+
+template <typename T>
+static T horner(T y, const double *c, int n)
+{
+    T acc = T(c[n - 1]);
+    for (int i = n - 2; i >= 0; --i) acc = T(c[i]) + y * acc;
+    return acc;
+}
+
+static std::complex<double> bessi0c(std::complex<double> ax)
+{
+    if (std::abs(ax) < 3.75) {
+        std::complex<double> y = ax / 3.75;
+        y = y * y;
+        return horner(y, kSmall, 7);
+    }
+    std::complex<double> y = 3.75 / ax;
+    std::complex<double> r = (std::exp(ax) / std::sqrt(ax)) * horner(y, kLarge, 9);
+    if (ax.real() == 0) r = 2.0 * r; // kernel.m:32-34
+    return r;
+}
+
+double bessi0_host(double ax) { return bessi0c(std::complex<double>(ax, 0.0)).real(); }
+
+static double kernel_host(double dist2, double alpha, double J)
+{
+    const double half = J / 2;
+    const double t = 1 - dist2 / (half * half);
+    const double den = bessi0_host(alpha);
+    if (t >= 0) return bessi0_host(alpha * std::sqrt(t)) / den;
+    std::complex<double> arg(0.0, alpha * std::sqrt(-t));
+    return (bessi0c(arg) / den).real();
+}
+
+// deap.m:2-36,97-98.  ifft(X*K, 2K, 'symmetric') of the (J+1)-sample kernel
+// table is 0.5*T0 + sum_{d>=1} T_d cos(pi d m / K); rows m in [-N/2, N/2) are
+// kept and fftshifted, so output index p holds m = p - N/2.  Returns 1/U.
+static std::vector<double> deap_host(const int N[3], const int K[3], double J, double alpha,
+                                     int radial, int is2d)
+{
+    const int nJ = (int)std::floor(J) + 1;
+    const int nz = is2d ? 1 : nJ;
+    std::vector<double> T((size_t)nJ * nJ * nz);
+    for (int dz = 0; dz < nz; ++dz)
+        for (int dy = 0; dy < nJ; ++dy)
+            for (int dx = 0; dx < nJ; ++dx) {
+                const double dx2 = (dx / 2.0) * (dx / 2.0), dy2 = (dy / 2.0) * (dy / 2.0),
+                             dz2 = (dz / 2.0) * (dz / 2.0);
+                double v;
+                if (radial)
+                    v = kernel_host(dx2 + dy2 + dz2, alpha, J);
+                else
+                    v = kernel_host(dx2, alpha, J) * kernel_host(dy2, alpha, J) *
+                        kernel_host(dz2, alpha, J);
+                T[((size_t)dz * nJ + dy) * nJ + dx] = v;
+            }
+    auto coef = [&](int axis, int d, int p) {
+        if (d == 0) return 0.5;
+        const double m = p - N[axis] / 2;
+        return std::cos(M_PI * d * m / K[axis]);
+    };
+    const int N1 = N[0], N2 = N[1], N3 = N[2];
+    // x
+    std::vector<double> A((size_t)N1 * nJ * nz, 0.0);
+    for (int dz = 0; dz < nz; ++dz)
+        for (int dy = 0; dy < nJ; ++dy)
+            for (int px = 0; px < N1; ++px) {
+                double s = 0;
+                for (int dx = 0; dx < nJ; ++dx) s += T[((size_t)dz * nJ + dy) * nJ + dx] * coef(0, dx, px);
+                A[((size_t)dz * nJ + dy) * N1 + px] = s;
+            }
+    // y
+    std::vector<double> B((size_t)N1 * N2 * nz, 0.0);
+    for (int dz = 0; dz < nz; ++dz)
+        for (int py = 0; py < N2; ++py)
+            for (int px = 0; px < N1; ++px) {
+                double s = 0;
+                for (int dy = 0; dy < nJ; ++dy) s += A[((size_t)dz * nJ + dy) * N1 + px] * coef(1, dy, py);
+                B[((size_t)dz * N2 + py) * N1 + px] = s;
+            }
+    std::vector<double> U((size_t)N1 * N2 * N3, 0.0);
+    if (is2d) {
+        for (size_t i = 0; i < U.size(); ++i) U[i] = 1.0 / B[i];
+        return U;
+    }
+    for (int pz = 0; pz < N3; ++pz)
+        for (int py = 0; py < N2; ++py)
+            for (int px = 0; px < N1; ++px) {
+                double s = 0;
+                for (int dz = 0; dz < nz; ++dz) s += B[((size_t)dz * N2 + py) * N1 + px] * coef(2, dz, pz);
+                U[((size_t)pz * N2 + py) * N1 + px] = 1.0 / s;
+            }
+    return U;
+}
+
+// ------------------------------------------------------ device kernels
+struct KeyParams {
+    double u;
+    int K[3], T[3], nt[3], Ra[3];
+    int is2d;
+    uint32_t ntiles;
+};
+
+__device__ __forceinline__ int64_t wrap64(int64_t x, int64_t K)
+{
+    int64_t r = x % K;
+    return r < 0 ? r + K : r;
+}
+
+// nufft_3d.m:120-125: om scaled by u in double; ok mask; tile key.
+__global__ void k_keys(const double *__restrict__ om, int64_t M, KeyParams kp,
+                       uint32_t *__restrict__ keys, int32_t *__restrict__ vals)
+{
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    double og[3];
+    bool ok = true;
+    for (int a = 0; a < 3; ++a) {
+        og[a] = kp.u * om[3 * m + a];
+        ok = ok && og[a] >= -kp.K[a] / 2.0 && og[a] <= kp.K[a] / 2.0 - 1;
+    }
+    if (kp.is2d) ok = true; // nufft_3d.m:125 ('... & ok | N(3)==1')
+    uint32_t key = kp.ntiles;
+    if (ok) {
+        int t[3];
+        for (int a = 0; a < 3; ++a) {
+            const int64_t b = wrap64((int64_t)round(og[a]), kp.K[a]);
+            t[a] = (int)(b / kp.T[a]);
+        }
+        key = (uint32_t)(t[0] + kp.nt[0] * (t[1] + kp.nt[1] * t[2]));
+    }
+    keys[m] = key;
+    vals[m] = (int32_t)m;
+}
+
+__global__ void k_hist(const uint32_t *__restrict__ keys, int64_t M, uint32_t ntiles,
+                       int32_t *__restrict__ counts)
+{
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    const uint32_t k = keys[m];
+    if (k < ntiles) atomicAdd(&counts[k], 1);
+}
+
+__global__ void k_records(const double *__restrict__ om, const int32_t *__restrict__ perm,
+                          int64_t nnz, KeyParams kp, float4 *__restrict__ samples,
+                          int32_t *__restrict__ inv)
+{
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nnz) return;
+    const int m = perm[s];
+    float f[3];
+    int l[3];
+    for (int a = 0; a < 3; ++a) {
+        const double og = kp.u * om[3 * (int64_t)m + a];
+        const double r = round(og);
+        f[a] = (float)(og - r);
+        const int64_t b = wrap64((int64_t)r, kp.K[a]);
+        const int64_t t = b / kp.T[a];
+        l[a] = (int)(b - t * kp.T[a]) + kp.Ra[a];
+    }
+    const int packed = l[0] | (l[1] << 8) | (l[2] << 16);
+    samples[s] = make_float4(f[0], f[1], f[2], __int_as_float(packed));
+    inv[m] = (int32_t)s;
+}
+
+__global__ void k_sorted_from_orig(const float *__restrict__ dorig, const int32_t *__restrict__ perm,
+                                   int64_t nnz, float *__restrict__ dsorted)
+{
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < nnz) dsorted[s] = dorig[perm[s]];
+}
+
+__global__ void k_orig_from_sorted(const float *__restrict__ dsorted, const int32_t *__restrict__ inv,
+                                   int64_t M, float *__restrict__ dorig)
+{
+    const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= M) return;
+    const int s = inv[m];
+    dorig[m] = s >= 0 ? dsorted[s] : 0.f;
+}
+
+// Count taps (nonzeros of H) per block, for the plan summary.
+template <int R>
+__global__ void k_count_taps(const float4 *__restrict__ samples, int64_t nnz, float half2, int radial,
+                             int rz, unsigned long long *__restrict__ total)
+{
+    const int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    unsigned long long c = 0;
+    if (s < nnz) {
+        const float4 r = samples[s];
+        for (int dz = -rz; dz <= rz; ++dz)
+            for (int dy = -R; dy <= R; ++dy)
+                for (int dx = -R; dx <= R; ++dx) {
+                    const float ex = dx - r.x, ey = dy - r.y, ez = dz - r.z;
+                    if (radial) c += (ez * ez + ey * ey) + ex * ex <= half2;
+                    else c += (ex * ex <= half2) && (ey * ey <= half2) && (ez * ez <= half2);
+                }
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(total, c);
+}
+
+// ---------------------------------------------------------------- host
+int configure_fft_kernels();
+int configure_interp_kernels();
+
+int configure_kernels()
+{
+    static std::mutex mu;
+    static int done_mask = 0; // per device bit (first 32 devices)
+    int dev = 0;
+    NUFFT_CUDA_TRY(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lk(mu);
+    if (dev < 32 && (done_mask & (1 << dev))) return NUFFT3D_SUCCESS;
+    NUFFT_TRY(configure_fft_kernels());
+    NUFFT_TRY(configure_interp_kernels());
+    if (dev < 32) done_mask |= 1 << dev;
+    return NUFFT3D_SUCCESS;
+}
+
+static void free_plan_memory(nufft3d_plan *p)
+{
+    auto F = [](void *ptr) {
+        if (ptr) cudaFree(ptr);
+    };
+    F(p->samples);
+    F(p->perm);
+    F(p->inv);
+    F(p->blocks);
+    F(p->U);
+    F(p->d);
+    F(p->d_orig);
+    F(p->wbuf);
+    for (int a = 0; a < 3; ++a) F(p->tw[a]);
+    F(p->scratch.B1);
+    F(p->scratch.B2);
+    if (p->scratch.G != p->scratch.B2) F(p->scratch.G); // 2D: G aliases B2
+    F(p->scratch.ks);
+    F(p->stage.in);
+    F(p->stage.out);
+    SolverWork &w = p->solver;
+    F(w.x); F(w.r); F(w.p); F(w.q); F(w.v); F(w.vprev); F(w.w1); F(w.w2);
+    F(w.partial); F(w.scal); F(w.iters);
+    if (p->own_stream) cudaStreamDestroy(p->own_stream);
+}
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev)
+    {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard()
+    {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+template <typename T>
+static int dmalloc(T **ptr, size_t count, int64_t *acc)
+{
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void **)ptr, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return fail(NUFFT3D_ERR_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+    }
+    if (acc) *acc += (int64_t)(count * sizeof(T));
+    return NUFFT3D_SUCCESS;
+}
+
+static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts &o)
+{
+    const int64_t M = p->M;
+    const Geom &g = p->geom;
+    cudaStream_t s = p->own_stream;
+    double *om_dev = nullptr;
+    NUFFT_TRY(dmalloc(&om_dev, (size_t)3 * M, nullptr));
+    struct Tmp {
+        std::vector<void *> ptrs;
+        ~Tmp()
+        {
+            for (void *q : ptrs) cudaFree(q);
+        }
+    } tmp;
+    tmp.ptrs.push_back(om_dev);
+    NUFFT_CUDA_TRY(cudaMemcpyAsync(om_dev, om_host, sizeof(double) * 3 * M, cudaMemcpyHostToDevice, s));
+
+    KeyParams kp;
+    kp.u = p->u;
+    kp.is2d = g.is2d;
+    for (int a = 0; a < 3; ++a) {
+        kp.K[a] = g.K[a];
+        kp.T[a] = g.T[a];
+        kp.nt[a] = g.nt[a];
+        kp.Ra[a] = g.Ra[a];
+    }
+    const uint64_t ntiles64 = (uint64_t)g.nt[0] * g.nt[1] * g.nt[2];
+    if (ntiles64 >= 0x7fffffffull) return fail(NUFFT3D_ERR_SIZE, "too many interpolation tiles");
+    kp.ntiles = (uint32_t)ntiles64;
+    const uint32_t ntiles = kp.ntiles;
+
+    uint32_t *keys = nullptr, *keys_sorted = nullptr;
+    int32_t *vals = nullptr;
+    NUFFT_TRY(dmalloc(&keys, (size_t)M, nullptr));
+    tmp.ptrs.push_back(keys);
+    NUFFT_TRY(dmalloc(&keys_sorted, (size_t)M, nullptr));
+    tmp.ptrs.push_back(keys_sorted);
+    NUFFT_TRY(dmalloc(&vals, (size_t)M, nullptr));
+    tmp.ptrs.push_back(vals);
+    NUFFT_TRY(dmalloc(&p->perm, (size_t)M, &p->table_bytes));
+    const int th = 256;
+    const unsigned nbM = (unsigned)((M + th - 1) / th);
+    if (M > 0) {
+        k_keys<<<nbM, th, 0, s>>>(om_dev, M, kp, keys, vals);
+        NUFFT_CUDA_TRY(cudaGetLastError());
+    }
+    int end_bit = 1;
+    while ((1ull << end_bit) <= (uint64_t)ntiles) ++end_bit;
+    size_t tb = 0;
+    NUFFT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tb, keys, keys_sorted, vals, p->perm,
+                                                   (int)M, 0, end_bit, s));
+    void *tstore = nullptr;
+    NUFFT_CUDA_TRY(cudaMalloc(&tstore, tb ? tb : 1));
+    tmp.ptrs.push_back(tstore);
+    NUFFT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(tstore, tb, keys, keys_sorted, vals, p->perm,
+                                                   (int)M, 0, end_bit, s));
+    int32_t *counts = nullptr;
+    NUFFT_TRY(dmalloc(&counts, (size_t)ntiles, nullptr));
+    tmp.ptrs.push_back(counts);
+    NUFFT_CUDA_TRY(cudaMemsetAsync(counts, 0, sizeof(int32_t) * ntiles, s));
+    if (M > 0) {
+        k_hist<<<nbM, th, 0, s>>>(keys, M, ntiles, counts);
+        NUFFT_CUDA_TRY(cudaGetLastError());
+    }
+    std::vector<int32_t> hc(ntiles);
+    NUFFT_CUDA_TRY(cudaMemcpyAsync(hc.data(), counts, sizeof(int32_t) * ntiles, cudaMemcpyDeviceToHost, s));
+    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    int64_t nnz = 0;
+    for (uint32_t t = 0; t < ntiles; ++t) nnz += hc[t];
+    p->nnz = nnz;
+
+    // tile pieces of at most S samples, split evenly
+    const int S = o.max_samples_per_block > 0 ? o.max_samples_per_block : 2048;
+    std::vector<int4> blocks;
+    int64_t off = 0;
+    for (uint32_t t = 0; t < ntiles; ++t) {
+        const int64_t c = hc[t];
+        if (c > 0) {
+            const int64_t nb = (c + S - 1) / S;
+            for (int64_t b = 0; b < nb; ++b) {
+                const int64_t b0 = c * b / nb, b1 = c * (b + 1) / nb;
+                blocks.push_back(make_int4((int)t, (int)(off + b0), (int)(b1 - b0), 0));
+            }
+        }
+        off += c;
+    }
+    // largest pieces first: the heavy centre of radial k-space starts early
+    std::stable_sort(blocks.begin(), blocks.end(), [](const int4 &a, const int4 &b) { return a.z > b.z; });
+    p->n_blocks = (int64_t)blocks.size();
+    NUFFT_TRY(dmalloc(&p->blocks, blocks.size(), &p->table_bytes));
+    if (!blocks.empty())
+        NUFFT_CUDA_TRY(cudaMemcpyAsync(p->blocks, blocks.data(), sizeof(int4) * blocks.size(),
+                                       cudaMemcpyHostToDevice, s));
+
+    NUFFT_TRY(dmalloc(&p->samples, (size_t)nnz, &p->table_bytes));
+    NUFFT_TRY(dmalloc(&p->inv, (size_t)M, &p->table_bytes));
+    NUFFT_CUDA_TRY(cudaMemsetAsync(p->inv, 0xFF, sizeof(int32_t) * (M > 0 ? M : 1), s));
+    if (nnz > 0) {
+        k_records<<<(unsigned)((nnz + th - 1) / th), th, 0, s>>>(om_dev, p->perm, nnz, kp, p->samples, p->inv);
+        NUFFT_CUDA_TRY(cudaGetLastError());
+        unsigned long long *tot = nullptr;
+        NUFFT_CUDA_TRY(cudaMalloc(&tot, sizeof(unsigned long long)));
+        tmp.ptrs.push_back(tot);
+        NUFFT_CUDA_TRY(cudaMemsetAsync(tot, 0, sizeof(unsigned long long), s));
+        const unsigned nbs = (unsigned)((nnz + th - 1) / th);
+        const int rz = g.is2d ? 0 : g.R;
+        switch (g.R) {
+        case 1: k_count_taps<1><<<nbs, th, 0, s>>>(p->samples, nnz, p->kb.half2, g.radial, rz, tot); break;
+        case 2: k_count_taps<2><<<nbs, th, 0, s>>>(p->samples, nnz, p->kb.half2, g.radial, rz, tot); break;
+        case 3: k_count_taps<3><<<nbs, th, 0, s>>>(p->samples, nnz, p->kb.half2, g.radial, rz, tot); break;
+        default: k_count_taps<4><<<nbs, th, 0, s>>>(p->samples, nnz, p->kb.half2, g.radial, rz, tot); break;
+        }
+        NUFFT_CUDA_TRY(cudaGetLastError());
+        unsigned long long ht = 0;
+        NUFFT_CUDA_TRY(cudaMemcpyAsync(&ht, tot, sizeof(ht), cudaMemcpyDeviceToHost, s));
+        NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+        p->taps = (double)ht / (double)nnz;
+    }
+
+    // deapodization (FP64 on the host, stored FP32 like deap.m:100-101)
+    {
+        std::vector<double> U = deap_host(p->N, g.K, p->J, p->alpha, g.radial, g.is2d);
+        std::vector<float> Uf(U.size());
+        for (size_t i = 0; i < U.size(); ++i) Uf[i] = (float)U[i];
+        NUFFT_TRY(dmalloc(&p->U, Uf.size(), &p->table_bytes));
+        NUFFT_CUDA_TRY(cudaMemcpyAsync(p->U, Uf.data(), sizeof(float) * Uf.size(), cudaMemcpyHostToDevice, s));
+        NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    // twiddles (FP64 -> FP32)
+    for (int a = 0; a < 3; ++a) {
+        const int K = g.K[a];
+        if (!fft_factor(K, p->fft[a]))
+            return fail(NUFFT3D_ERR_UNSUPPORTED,
+                        "oversampled size K=" + std::to_string(K) +
+                            " has a prime factor above 13 (FFT radices 2,3,5,7,11,13)");
+        std::vector<float2> tw(K);
+        for (int j = 0; j < K; ++j) {
+            const double ang = -2.0 * M_PI * (double)j / (double)K;
+            tw[j] = make_float2((float)std::cos(ang), (float)std::sin(ang));
+        }
+        NUFFT_TRY(dmalloc(&p->tw[a], (size_t)K, &p->table_bytes));
+        NUFFT_CUDA_TRY(cudaMemcpyAsync(p->tw[a], tw.data(), sizeof(float2) * K, cudaMemcpyHostToDevice, s));
+        p->fft[a].tw = p->tw[a];
+        NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    // density: user supplied (nufft_3d.m:229-237) or density.m
+    NUFFT_TRY(dmalloc(&p->d, (size_t)nnz, &p->table_bytes));
+    NUFFT_TRY(dmalloc(&p->d_orig, (size_t)M, &p->table_bytes));
+    if (o.d) {
+        NUFFT_CUDA_TRY(cudaMemcpyAsync(p->d_orig, o.d, sizeof(float) * M, cudaMemcpyHostToDevice, s));
+        if (nnz > 0) {
+            k_sorted_from_orig<<<(unsigned)((nnz + th - 1) / th), th, 0, s>>>(p->d_orig, p->perm, nnz, p->d);
+            NUFFT_CUDA_TRY(cudaGetLastError());
+        }
+        if (M > 0) {
+            k_orig_from_sorted<<<nbM, th, 0, s>>>(p->d, p->inv, M, p->d_orig); // d(~ok) = 0
+            NUFFT_CUDA_TRY(cudaGetLastError());
+        }
+        NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    } else {
+        const int iters = o.density_iters > 0 ? o.density_iters : (o.density_iters == 0 ? 20 : 0);
+        NUFFT_TRY(run_density(p, iters, s));
+    }
+    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    return NUFFT3D_SUCCESS;
+}
+
+int refresh_density_orig(nufft3d_plan *p, cudaStream_t s)
+{
+    if (p->M == 0) return NUFFT3D_SUCCESS;
+    const int th = 256;
+    k_orig_from_sorted<<<(unsigned)((p->M + th - 1) / th), th, 0, s>>>(p->d, p->inv, p->M, p->d_orig);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
+} // namespace nufft3d
+
+using namespace nufft3d;
+
+extern "C" int nufft3d_opts_default(nufft3d_opts *o)
+{
+    if (!o) return fail(NUFFT3D_ERR_ARG, "opts is NULL");
+    std::memset(o, 0, sizeof(*o));
+    o->J = 4;
+    o->u = 2;
+    o->alpha = 0;
+    o->radial = 1;
+    o->gpu = 1;
+    o->device = -1;
+    o->d = nullptr;
+    o->density_iters = 20;
+    return NUFFT3D_SUCCESS;
+}
+
+extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *Nin, int n_N,
+                                   const nufft3d_opts *opts_in, nufft3d_plan **out)
+{
+    clear_error();
+    if (!out) return fail(NUFFT3D_ERR_ARG, "plan output pointer is NULL");
+    *out = nullptr;
+    nufft3d_opts o;
+    if (opts_in) o = *opts_in;
+    else nufft3d_opts_default(&o);
+    // nufft_3d.m:60-61
+    if (!om || M <= 0) return fail(NUFFT3D_ERR_ARG, "om must be a real array with leading dimension of 3");
+    if (M > 0x7fffffffll) return fail(NUFFT3D_ERR_SIZE, "more than 2^31-1 samples");
+    for (int64_t i = 0; i < 3 * M; ++i)
+        if (!std::isfinite(om[i])) return fail(NUFFT3D_ERR_ARG, "om must be finite");
+    if (o.gpu == 0) return fail(NUFFT3D_ERR_UNSUPPORTED, "gpu=0 (CPU path) is not provided by this library");
+    if (o.gpu != 1) return fail(NUFFT3D_ERR_UNSUPPORTED, "only gpu=1 (single precision GPU) is implemented");
+    // nufft_3d.m:82-84
+    if (!(o.u >= 1 && o.u <= 6)) return fail(NUFFT3D_ERR_ARG, "value of u=" + std::to_string(o.u) + " is not recommended");
+    if (!(o.J > 0)) return fail(NUFFT3D_ERR_ARG, "J must be positive");
+    const int R = (int)std::ceil(o.J / 2);
+    if (R < 1 || R > 4) return fail(NUFFT3D_ERR_UNSUPPORTED, "J must satisfy ceil(J/2) <= 4 (J <= 8)");
+    // nufft_3d.m:85-92
+    double alpha = o.alpha;
+    if (alpha == 0) {
+        const double q = o.J * o.J * (1 - 0.5 / o.u) * (1 - 0.5 / o.u);
+        alpha = M_PI * std::sqrt(o.radial ? q - 0.6 * o.u : q - 0.8);
+    }
+    if (!(alpha > 0) || !std::isfinite(alpha)) return fail(NUFFT3D_ERR_ARG, "invalid Kaiser-Bessel alpha");
+    // nufft_3d.m:96-106
+    if (!Nin || !(n_N == 1 || n_N == 3)) return fail(NUFFT3D_ERR_ARG, "N must be scalar or 3-vector of even integers");
+    int N[3];
+    for (int a = 0; a < 3; ++a) N[a] = n_N == 1 ? Nin[0] : Nin[a];
+    if ((N[0] == 0 && N[1] == 0 && N[2] == 0) || N[0] % 2 || N[1] % 2 || N[0] <= 0 || N[1] <= 0 || N[2] < 0)
+        return fail(NUFFT3D_ERR_ARG, "N must be an even integer");
+    bool all_z0 = true;
+    for (int64_t m = 0; m < M && all_z0; ++m) all_z0 = om[3 * m + 2] == 0;
+    if (all_z0) N[2] = 1;
+    const int is2d = N[2] == 1;
+    if (!is2d && (N[2] % 2 || N[2] <= 0)) return fail(NUFFT3D_ERR_ARG, "N must be an even integer");
+    // nufft_3d.m:109-111
+    int K[3];
+    for (int a = 0; a < 3; ++a) K[a] = 2 * (int)std::ceil(N[a] * o.u / 2);
+    if (is2d) K[2] = 1;
+    if ((double)K[0] * K[1] * K[2] >= 2147483647.0) return fail(NUFFT3D_ERR_SIZE, "N or u too large");
+
+    int dev = o.device;
+    if (dev < 0) {
+        if (cudaGetDevice(&dev) != cudaSuccess) return fail(NUFFT3D_ERR_CUDA, "no CUDA device");
+    }
+    DeviceGuard guard(dev);
+    NUFFT_TRY(configure_kernels());
+
+    nufft3d_plan *p = new nufft3d_plan();
+    p->device = dev;
+    for (int a = 0; a < 3; ++a) p->N[a] = N[a];
+    p->M = M;
+    p->J = o.J;
+    p->u = o.u;
+    p->alpha = alpha;
+    p->radial = o.radial ? 1 : 0;
+    p->i0a = bessi0_host(alpha);
+    Geom &g = p->geom;
+    g.R = R;
+    g.radial = p->radial;
+    g.is2d = is2d;
+    for (int a = 0; a < 3; ++a) {
+        g.K[a] = K[a];
+        g.Ra[a] = (a == 2 && is2d) ? 0 : R;
+        int t = o.tile[a] > 0 ? o.tile[a] : (is2d ? (a == 2 ? 1 : 32) : 8);
+        if (a == 2 && is2d) t = 1;
+        if (t > 64) t = 64;
+        g.T[a] = t;
+        g.P[a] = t + 2 * g.Ra[a];
+        g.nt[a] = (K[a] + t - 1) / t;
+    }
+    KBParams &kb = p->kb;
+    const double half = o.J / 2;
+    kb.alpha = (float)alpha;
+    kb.inv_half2 = (float)(1.0 / (half * half));
+    kb.a2_over = (float)(alpha * alpha / (3.75 * 3.75));
+    kb.inv_i0a = (float)(1.0 / p->i0a);
+    kb.exp_over_i0a = (float)(std::exp(alpha) / p->i0a);
+    kb.half2 = (float)(half * half);
+    int cpp = o.max_coils_per_pass > 0 ? o.max_coils_per_pass : 8;
+    int cb = 1;
+    while (cb * 2 <= cpp && cb < 8) cb *= 2;
+    while (cb > 1 && smem_interp_bytes(g, cb) > 200 * 1024) cb /= 2;
+    if (smem_interp_bytes(g, cb) > 227 * 1024) {
+        delete p;
+        return fail(NUFFT3D_ERR_UNSUPPORTED, "interpolation tile too large for shared memory");
+    }
+    p->coils_per_pass = cb;
+    if (cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        delete p;
+        return fail(NUFFT3D_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    int st = build_plan(p, om, o);
+    if (st != NUFFT3D_SUCCESS) {
+        std::string msg = nufft3d_last_error();
+        free_plan_memory(p);
+        delete p;
+        return fail(st, msg);
+    }
+    if (o.verbose) {
+        std::printf(" Created nufft_3d plan: N=[%d %d %d] K=[%d %d %d] J=%g u=%g alpha=%g radial=%d\n",
+                    N[0], N[1], N[2], K[0], K[1], K[2], o.J, o.u, alpha, p->radial);
+        std::printf("  %lld points (out of %lld) are within bounds; %.2f taps/sample; %lld blocks\n",
+                    (long long)p->nnz, (long long)M, p->taps, (long long)p->n_blocks);
+    }
+    *out = p;
+    return NUFFT3D_SUCCESS;
+}
+
+extern "C" int nufft3d_plan_destroy(nufft3d_plan *p)
+{
+    clear_error();
+    if (!p) return NUFFT3D_SUCCESS;
+    {
+        DeviceGuard guard(p->device);
+        cudaDeviceSynchronize();
+        free_plan_memory(p);
+    }
+    delete p;
+    return NUFFT3D_SUCCESS;
+}
+
+extern "C" int nufft3d_plan_info(const nufft3d_plan *p, nufft3d_info *info)
+{
+    clear_error();
+    if (!p || !info) return fail(NUFFT3D_ERR_ARG, "NULL argument");
+    for (int a = 0; a < 3; ++a) {
+        info->N[a] = p->N[a];
+        info->K[a] = p->geom.K[a];
+        info->tile[a] = p->geom.T[a];
+    }
+    info->M = p->M;
+    info->nnz = p->nnz;
+    info->J = p->J;
+    info->u = p->u;
+    info->alpha = p->alpha;
+    info->radial = p->radial;
+    info->n_blocks = p->n_blocks;
+    info->taps_per_sample = p->taps;
+    info->device_bytes = p->table_bytes + (int64_t)p->scratch.bytes;
+    return NUFFT3D_SUCCESS;
+}
+
+extern "C" int nufft3d_get_deap(const nufft3d_plan *p, float *U)
+{
+    clear_error();
+    if (!p || !U) return fail(NUFFT3D_ERR_ARG, "NULL argument");
+    DeviceGuard guard(p->device);
+    const size_t n = (size_t)p->N[0] * p->N[1] * p->N[2];
+    NUFFT_CUDA_TRY(cudaMemcpy(U, p->U, n * sizeof(float), cudaMemcpyDeviceToHost));
+    return NUFFT3D_SUCCESS;
+}
+
+extern "C" int nufft3d_get_density(const nufft3d_plan *p, float *d)
+{
+    clear_error();
+    if (!p || !d) return fail(NUFFT3D_ERR_ARG, "NULL argument");
+    DeviceGuard guard(p->device);
+    NUFFT_CUDA_TRY(cudaMemcpy(d, p->d_orig, (size_t)p->M * sizeof(float), cudaMemcpyDeviceToHost));
+    return NUFFT3D_SUCCESS;
+}
+
+extern "C" const char *nufft3d_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" const char *nufft3d_version(void) { return "nufft3d-gb300 0.1 (sm_103a)"; }

@@ -1,0 +1,87 @@
+"""CPU tests of the C ABI: the library loads, exports every declared entry
+point, and rejects the reference's invalid arguments before touching a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from nufft_3d_gb300 import _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "nufft3d.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(nufft3d_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_library_exports_every_declared_symbol():
+    L = _lib.load()
+    names = declared_functions()
+    assert len(names) >= 15
+    for n in names:
+        assert hasattr(L, n), n
+    assert set(names) == set(_lib.SIGNATURES), set(names) ^ set(_lib.SIGNATURES)
+
+
+def test_opts_struct_layout_matches_defaults():
+    L = _lib.load()
+    o = _lib.Opts()
+    assert L.nufft3d_opts_default(ctypes.byref(o)) == 0
+    assert (o.J, o.u, o.alpha, o.radial, o.gpu, o.density_iters) == (4.0, 2.0, 0.0, 1, 1, 20)
+
+
+def _create(om, N, **kw):
+    L = _lib.load()
+    o = _lib.Opts()
+    L.nufft3d_opts_default(ctypes.byref(o))
+    for k, v in kw.items():
+        setattr(o, k, v)
+    om = np.ascontiguousarray(np.asarray(om, dtype=np.float64).T)
+    Nc = (ctypes.c_int32 * 3)(*np.resize(np.asarray(N, dtype=np.int32), 3))
+    plan = ctypes.c_void_p()
+    st = L.nufft3d_plan_create(om.ctypes.data, om.shape[0], ctypes.cast(Nc, ctypes.c_void_p), np.size(N),
+                               ctypes.byref(o), ctypes.byref(plan))
+    return st, _lib.last_error()
+
+
+@pytest.mark.parametrize("kw,N,code,msg", [
+    (dict(u=0.5), 16, _lib.ERR_ARG, "value of u"),          # nufft_3d.m:82-83
+    (dict(u=7.0), 16, _lib.ERR_ARG, "value of u"),
+    ({}, 15, _lib.ERR_ARG, "even integer"),                 # nufft_3d.m:101-102
+    ({}, [16, 15, 16], _lib.ERR_ARG, "even integer"),
+    (dict(gpu=0), 16, _lib.ERR_UNSUPPORTED, "CPU"),         # no CPU fallback
+    (dict(J=9.0), 16, _lib.ERR_UNSUPPORTED, "J"),
+])
+def test_invalid_arguments_rejected(kw, N, code, msg):
+    om = np.random.default_rng(0).uniform(-4, 4, (3, 50))
+    st, err = _create(om, N, **kw)
+    assert st == code and msg in err
+
+
+def test_too_large_grid_rejected():
+    # nufft_3d.m:111: prod(K) >= intmax('int32')
+    om = np.random.default_rng(0).uniform(-4, 4, (3, 50))
+    st, err = _create(om, 1024, u=2.0)
+    assert st == _lib.ERR_SIZE and "too large" in err
+
+
+def test_empty_trajectory_rejected():
+    st, err = _create(np.zeros((3, 0)), 16)
+    assert st == _lib.ERR_ARG and "om must be" in err
+
+
+def test_python_class_argument_checks():
+    from nufft_3d_gb300 import nufft_3d
+    with pytest.raises(ValueError, match="leading dimension of 3"):
+        nufft_3d(np.zeros((2, 4)), 16)
+    with pytest.raises(ValueError, match="string/value pairs"):
+        nufft_3d(np.ones((3, 4)), 16, "J")
+    with pytest.raises(ValueError, match="unknown property"):
+        nufft_3d(np.ones((3, 4)), 16, "K", 3)
+    with pytest.raises(_lib.NufftError, match="value of u"):
+        nufft_3d(np.ones((3, 4)), 16, "u", 9)
