@@ -1,0 +1,322 @@
+"""Benchmark: fwd+adj NUFFT throughput at 128^3 (8 coils) on one GB300.
+
+Workload (the single-GPU configuration the headline metric is quoted on):
+N = 128^3 image, u = 2 (K = 256^3), Kaiser-Bessel J = 6 radial kernel,
+3-D golden-angle koosh ball with 256 samples/spoke x 32768 spokes
+(M = 8,388,608 samples), 8 coils (modified Shepp-Logan phantom with phase
+times Gaussian coil maps), complex64.
+
+One step = fNUFT of all coils + aNUFT of all coils.
+  value   -- M*nc/t in Msample/s, inputs resident in HBM, device pointers
+             through the C ABI (nufft3d_forward / nufft3d_adjoint);
+  e2e     -- the same through the host-pointer entry points
+             (nufft3d_forward_host / nufft3d_adjoint_host) from pinned host
+             memory, every copy inside the timed region.
+The grid (1.07 GB) and the samples (0.54 GB) are far larger than L2, so no
+flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference's sparse path
+(oracle/, FP64, all host threads) on a bounded sample of the same workload.
+Multi-GPU: replicas only (one independent workload per rank, no collective on
+the data path; value = all ranks' samples / max time).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "fwd+adj NUFFT Msample/s at 128^3"
+WORKLOAD = "config2: N=128^3, u=2 (K=256^3), J=6 radial KB, koosh ball 256x32768 (M=8388608), 8 coils, complex64"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out = ""
+
+    def summary(self):
+        rows = []
+        for line in (self.out or "").strip().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), parts[3:7]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, r in rows for i, v in enumerate(r) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def stage_bytes(obj, nc):
+    """Algorithmic bytes per launch of each stage (reads + writes of its inputs/outputs)."""
+    N1, N2, N3 = (int(v) for v in obj.N)
+    K1, K2, K3 = (int(v) for v in obj.K)
+    M, nnz = obj.M, obj.nnz
+    c = 8 * nc
+    img, u = N1 * N2 * N3, N1 * N2 * N3 * 4
+    b1, b2, g = K1 * N2 * N3, K1 * K2 * N3, K1 * K2 * K3
+    return {
+        "fft_x_fwd": img * c + u + b1 * c,
+        "fft_y_fwd": b1 * c + b2 * c,
+        "fft_z_fwd": b2 * c + g * c,
+        "gather": g * c + nnz * 16 + nnz * c,
+        "permute_out": nnz * c + M * 4 + M * c,
+        "permute_in": M * c + M * 4 + nnz * c,
+        "grid_zero": g * c,
+        "spread": nnz * c + nnz * 16 + g * c,
+        "fft_z_adj": g * c + b2 * c,
+        "fft_y_adj": b2 * c + b1 * c,
+        "fft_x_adj": b1 * c + u + img * c,
+    }
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` at this workload from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "traffic_config2.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        return json.load(f).get(kernel)
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0
+    import torch
+    import torch.distributed as dist
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl")
+    return rank, ws, local
+
+
+def max_over_ranks(x, ws):
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def build_inputs(N, n_read, n_spokes, nc):
+    from nufft_3d_gb300 import synth
+    om = synth.koosh_ball(N, n_read, n_spokes)
+    im = synth.phantom_with_phase(N)[..., None] * synth.coil_maps(N, nc)
+    return om, im.astype(np.complex64)
+
+
+def cpu_baseline(om, N, n_read, nc, steps=3):
+    from oracle import cpu_bench
+    return cpu_bench.run(om, N, n_read, nc, steps)
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    om, _ = build_inputs(args.N, args.n_read, args.n_spokes, args.nc)
+    from oracle import cpu_bench
+    r = cpu_bench.run(om, args.N, args.n_read, args.nc, max(1, args.warmup) + args.steps)
+    v = r["value"]
+    line = {"metric": METRIC, "value": v, "unit": "Msample/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": r["sec_per_coil_step"] * args.nc * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": WORKLOAD, "l2": "inputs larger than L2"},
+            "cpu_baseline": {"value": v, "unit": "Msample/s", "cores": r["cores"], "kind": r["kind"],
+                             "sample": r["sample"]},
+            "e2e": {"value": v, "unit": "Msample/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--N", type=int, default=128)
+    ap.add_argument("--n-read", dest="n_read", type=int, default=256)
+    ap.add_argument("--n-spokes", dest="n_spokes", type=int, default=32768)
+    ap.add_argument("--nc", type=int, default=8)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tile", type=str, default=None)
+    ap.add_argument("--coils-per-pass", type=int, default=0)
+    ap.add_argument("--samples-per-block", type=int, default=0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    from nufft_3d_gb300 import _lib, nufft_3d
+
+    rank, ws, local = dist_init()
+    torch.cuda.set_device(local)
+    om, im = build_inputs(args.N, args.n_read, args.n_spokes, args.nc)
+    tile = tuple(int(t) for t in args.tile.split(",")) if args.tile else None
+    obj = nufft_3d(om, args.N, "J", 6, "u", 2, device=local, tile=tile, coils_per_pass=args.coils_per_pass,
+                   samples_per_block=args.samples_per_block)
+    L, plan = obj._L, obj.plan
+    nc, M = args.nc, obj.M
+    x = torch.from_numpy(np.ascontiguousarray(im.transpose(3, 2, 1, 0))).cuda()
+    k = torch.empty((nc, M), dtype=torch.complex64, device="cuda")
+    x2 = torch.empty_like(x)
+    stream = torch.cuda.current_stream()
+    sp = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        _lib.check(L.nufft3d_forward(plan, x.data_ptr(), k.data_ptr(), nc, sp))
+        _lib.check(L.nufft3d_adjoint(plan, k.data_ptr(), x2.data_ptr(), nc, sp))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(ws)
+    torch.cuda.synchronize()
+    _lib.check(L.nufft3d_profile(plan, 1))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    buf = ctypes.create_string_buffer(8192)
+    _lib.check(L.nufft3d_profile_read(plan, buf, 8192))
+    _lib.check(L.nufft3d_profile(plan, 0))
+    prof = json.loads(buf.value.decode())
+    barrier(ws)
+    ms_max = max_over_ranks(ms, ws)
+    value = M * nc * args.steps * ws / (ms_max / 1e3) / 1e6
+
+    # e2e: host-pointer entry points, pinned host buffers, copies inside the timed region
+    xh = torch.from_numpy(np.ascontiguousarray(im.transpose(3, 2, 1, 0))).pin_memory()
+    kh = torch.empty((nc, M), dtype=torch.complex64).pin_memory()
+    x2h = torch.empty_like(xh).pin_memory()
+
+    def step_host():
+        _lib.check(L.nufft3d_forward_host(plan, xh.data_ptr(), kh.data_ptr(), nc))
+        _lib.check(L.nufft3d_adjoint_host(plan, kh.data_ptr(), x2h.data_ptr(), nc))
+
+    for _ in range(args.warmup):
+        step_host()
+    torch.cuda.synchronize()
+    barrier(ws)
+    e_steps = max(3, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e_steps):
+        step_host()
+    torch.cuda.synchronize()
+    t_e2e = time.perf_counter() - t0
+    t_e2e = max_over_ranks(t_e2e, ws)
+    e2e = M * nc * e_steps * ws / t_e2e / 1e6
+    h2d = (x.numel() + k.numel()) * 8
+    d2h = (k.numel() + x.numel()) * 8
+
+    # roofline of the dominant stage
+    hbm, src = peaks()
+    sb = stage_bytes(obj, nc)
+    stages = {}
+    for name, r in prof.items():
+        if r["launches"] == 0:
+            stages[name] = {"ms_per_step": r["ms"] / args.steps, "launches": 0, "note": "cudaMemsetAsync"}
+            continue
+        per_launch_ms = r["ms"] / r["launches"]
+        gbs = sb[name] / (per_launch_ms / 1e3) / 1e9 / (r["launches"] / r["calls"])
+        stages[name] = {"ms_per_step": r["ms"] / args.steps, "launches": r["launches"],
+                        "algo_bytes_per_launch": sb[name] // max(1, r["launches"] // r["calls"]),
+                        "achieved_gbs": round(gbs, 1), "frac_of_%s_hbm" % src: round(gbs / hbm, 4)}
+    dom = max((n for n in stages if stages[n]["launches"]), key=lambda n: stages[n]["ms_per_step"])
+    d = stages[dom]
+    roof = {"bound": "hbm", "kernel": dom, "achieved": d["achieved_gbs"], "peak": hbm, "unit": "GB/s",
+            "frac": round(d["achieved_gbs"] / hbm, 4), "peak_source": src,
+            "traffic": ncu_traffic(dom), "algo_bytes_per_launch": d["algo_bytes_per_launch"]}
+    launches = sum(r["launches"] for r in prof.values())
+
+    if rank != 0:
+        return 0
+    line = {"metric": METRIC, "value": round(value, 2), "unit": "Msample/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms_max / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64 (fp32)",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "N": args.N, "M": M, "nnz": obj.nnz, "nc": nc,
+                       "taps_per_sample": round(obj.taps_per_sample, 2), "tile": list(obj.tile),
+                       "blocks": obj.n_blocks, "l2": "inputs larger than L2 (grid 1.07 GB), no flush",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "e2e": {"value": round(e2e, 2), "unit": "Msample/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "api": "nufft3d_forward_host + nufft3d_adjoint_host, pinned"},
+            "gpu_launches": launches,
+            "roofline": roof,
+            "stages": stages,
+            "clocks": clk.summary()}
+    if not args.no_cpu_baseline and ws == 1:
+        line["cpu_baseline"] = cpu_baseline(om, args.N, args.n_read, nc)
+    print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -135,6 +135,17 @@ int nufft3d_inverse_host(nufft3d_plan *plan, const float *raw_host, float *x_hos
 /* Re-runs density.m on the plan (maxit iterations) and stores it as obj.d. */
 int nufft3d_density(nufft3d_plan *plan, int maxit);
 
+/* Stage timing with CUDA events on the launching stream (the reference's
+ * tic/toc around its phases, nufft_3d.m:130,213 and iNUFT.m:117,227).
+ * enable = 1 starts (and resets) timing, 0 stops it.  Stages captured into a
+ * CUDA graph are not timed. */
+int nufft3d_profile(nufft3d_plan *plan, int enable);
+
+/* Writes the accumulated stage times as a JSON object into buf:
+ * {"gather": {"calls": C, "launches": L, "ms": T}, ...}.  Synchronises on the
+ * recorded events. */
+int nufft3d_profile_read(nufft3d_plan *plan, char *buf, int cap);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char *nufft3d_last_error(void);
 

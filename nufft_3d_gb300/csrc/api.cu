@@ -2,6 +2,8 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdio>
+#include <cstring>
 #include <string>
 
 #include "internal.h"
@@ -61,13 +63,94 @@ static size_t grid_bytes(const nufft3d_plan *p, int nc)
     return (size_t)p->geom.K[0] * p->geom.K[1] * p->geom.K[2] * nc * sizeof(float2);
 }
 
+// ------------------------------------------------------------ profiling
+const char *const kStageNames[ST_COUNT] = {"fft_x_fwd", "fft_y_fwd", "fft_z_fwd", "gather",
+                                           "permute_out", "permute_in", "grid_zero", "spread",
+                                           "fft_z_adj", "fft_y_adj", "fft_x_adj"};
+
+static cudaEvent_t pool_get(Profiler &pr)
+{
+    if (!pr.pool.empty()) {
+        cudaEvent_t e = pr.pool.back();
+        pr.pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+    return e;
+}
+
+StageTimer::StageTimer(nufft3d_plan *p_, int stage_, int launches_, cudaStream_t s_)
+    : p(p_), stage(stage_), launches(launches_), s(s_)
+{
+    if (!p->prof.on) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+    a = pool_get(p->prof);
+    if (a) cudaEventRecord(a, s);
+}
+
+StageTimer::~StageTimer()
+{
+    if (!a) return;
+    cudaEvent_t b = pool_get(p->prof);
+    if (!b) return;
+    cudaEventRecord(b, s);
+    p->prof.pending.push_back({stage, launches, a, b});
+}
+
+int profile_resolve(nufft3d_plan *p)
+{
+    Profiler &pr = p->prof;
+    for (auto &r : pr.pending) {
+        NUFFT_CUDA_TRY(cudaEventSynchronize(r.b));
+        float ms = 0;
+        NUFFT_CUDA_TRY(cudaEventElapsedTime(&ms, r.a, r.b));
+        pr.ms[r.stage] += ms;
+        pr.launches[r.stage] += r.launches;
+        pr.calls[r.stage] += 1;
+        pr.pool.push_back(r.a);
+        pr.pool.push_back(r.b);
+    }
+    pr.pending.clear();
+    return NUFFT3D_SUCCESS;
+}
+
+void profile_release(nufft3d_plan *p)
+{
+    Profiler &pr = p->prof;
+    for (auto &r : pr.pending) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    pr.pending.clear();
+    for (auto e : pr.pool) cudaEventDestroy(e);
+    pr.pool.clear();
+}
+
+int coil_passes(const nufft3d_plan *p, int nc)
+{
+    int n = 0;
+    for (int c0 = 0; c0 < nc; c0 += p->coils_per_pass) ++n;
+    return n;
+}
+
 // image -> grid G (fft3_pad of U.*x)
 static int to_grid(nufft3d_plan *p, const float2 *x, int nc, cudaStream_t s)
 {
     Scratch &S = p->scratch;
-    NUFFT_TRY(launch_fx(p, x, S.B1, nc, s));
-    NUFFT_TRY(launch_fy(p, S.B1, S.B2, nc, s));
-    if (!p->geom.is2d) NUFFT_TRY(launch_fz(p, S.B2, S.G, nc, s));
+    {
+        StageTimer t(p, ST_FFT_X_FWD, 1, s);
+        NUFFT_TRY(launch_fx(p, x, S.B1, nc, s));
+    }
+    {
+        StageTimer t(p, ST_FFT_Y_FWD, 1, s);
+        NUFFT_TRY(launch_fy(p, S.B1, S.B2, nc, s));
+    }
+    if (!p->geom.is2d) {
+        StageTimer t(p, ST_FFT_Z_FWD, 1, s);
+        NUFFT_TRY(launch_fz(p, S.B2, S.G, nc, s));
+    }
     return NUFFT3D_SUCCESS;
 }
 
@@ -76,10 +159,35 @@ static int from_grid(nufft3d_plan *p, float2 *x, int nc, float scale, const floa
                      float add_coef, cudaStream_t s)
 {
     Scratch &S = p->scratch;
-    if (!p->geom.is2d) NUFFT_TRY(launch_iz(p, S.G, S.B2, nc, s));
-    NUFFT_TRY(launch_iy(p, S.B2, S.B1, nc, s));
-    NUFFT_TRY(launch_ix(p, S.B1, x, nc, scale, addend, add_coef, s));
+    if (!p->geom.is2d) {
+        StageTimer t(p, ST_FFT_Z_ADJ, 1, s);
+        NUFFT_TRY(launch_iz(p, S.G, S.B2, nc, s));
+    }
+    {
+        StageTimer t(p, ST_FFT_Y_ADJ, 1, s);
+        NUFFT_TRY(launch_iy(p, S.B2, S.B1, nc, s));
+    }
+    {
+        StageTimer t(p, ST_FFT_X_ADJ, 1, s);
+        NUFFT_TRY(launch_ix(p, S.B1, x, nc, scale, addend, add_coef, s));
+    }
     return NUFFT3D_SUCCESS;
+}
+
+static int gather_timed(nufft3d_plan *p, int nc, float scale, const float *ws, cudaStream_t s)
+{
+    StageTimer t(p, ST_GATHER, coil_passes(p, nc), s);
+    return launch_gather(p, p->scratch.G, p->scratch.ks, nc, scale, ws, s);
+}
+
+static int spread_timed(nufft3d_plan *p, int nc, cudaStream_t s)
+{
+    {
+        StageTimer t(p, ST_GRID_ZERO, 0, s);
+        NUFFT_CUDA_TRY(cudaMemsetAsync(p->scratch.G, 0, grid_bytes(p, nc), s));
+    }
+    StageTimer t(p, ST_SPREAD, coil_passes(p, nc), s);
+    return launch_spread(p, p->scratch.ks, p->scratch.G, nc, s);
 }
 
 int op_forward(nufft3d_plan *p, const float2 *x, float2 *k, int nc, cudaStream_t s)
@@ -90,8 +198,8 @@ int op_forward(nufft3d_plan *p, const float2 *x, float2 *k, int nc, cudaStream_t
         return NUFFT3D_SUCCESS;
     }
     NUFFT_TRY(to_grid(p, x, nc, s));
-    NUFFT_TRY(launch_gather(p, p->scratch.G, p->scratch.ks, nc, (float)(1.0 / std::sqrt((double)p->nnz)),
-                            nullptr, s));
+    NUFFT_TRY(gather_timed(p, nc, (float)(1.0 / std::sqrt((double)p->nnz)), nullptr, s));
+    StageTimer t(p, ST_PERMUTE_OUT, 1, s);
     NUFFT_TRY(launch_permute_out(p, p->scratch.ks, k, nc, 1.f, s));
     return NUFFT3D_SUCCESS;
 }
@@ -104,9 +212,11 @@ int op_adjoint_weighted(nufft3d_plan *p, const float2 *k, float2 *x, int nc, con
         NUFFT_CUDA_TRY(cudaMemsetAsync(x, 0, img_elems(p) * nc * sizeof(float2), s));
         return NUFFT3D_SUCCESS;
     }
-    NUFFT_TRY(launch_permute_in(p, k, p->scratch.ks, nc, wsorted, s));
-    NUFFT_CUDA_TRY(cudaMemsetAsync(p->scratch.G, 0, grid_bytes(p, nc), s));
-    NUFFT_TRY(launch_spread(p, p->scratch.ks, p->scratch.G, nc, s));
+    {
+        StageTimer t(p, ST_PERMUTE_IN, 1, s);
+        NUFFT_TRY(launch_permute_in(p, k, p->scratch.ks, nc, wsorted, s));
+    }
+    NUFFT_TRY(spread_timed(p, nc, s));
     NUFFT_TRY(from_grid(p, x, nc, (float)(1.0 / std::sqrt((double)p->nnz)), nullptr, 0.f, s));
     return NUFFT3D_SUCCESS;
 }
@@ -128,10 +238,8 @@ int op_normal(nufft3d_plan *p, const float2 *x, float2 *y, int nc, double damp,
         return NUFFT3D_SUCCESS;
     }
     NUFFT_TRY(to_grid(p, x, nc, s));
-    NUFFT_TRY(launch_gather(p, p->scratch.G, p->scratch.ks, nc, (float)(1.0 / (double)p->nnz),
-                            wsorted ? wsorted : p->d, s));
-    NUFFT_CUDA_TRY(cudaMemsetAsync(p->scratch.G, 0, grid_bytes(p, nc), s));
-    NUFFT_TRY(launch_spread(p, p->scratch.ks, p->scratch.G, nc, s));
+    NUFFT_TRY(gather_timed(p, nc, (float)(1.0 / (double)p->nnz), wsorted ? wsorted : p->d, s));
+    NUFFT_TRY(spread_timed(p, nc, s));
     NUFFT_TRY(from_grid(p, y, nc, 1.f, x, d2, s));
     return NUFFT3D_SUCCESS;
 }
@@ -320,5 +428,44 @@ extern "C" int nufft3d_density(nufft3d_plan *p, int maxit)
     DevGuard g(p->device);
     NUFFT_TRY(run_density(p, maxit, p->own_stream));
     NUFFT_CUDA_TRY(cudaStreamSynchronize(p->own_stream));
+    return NUFFT3D_SUCCESS;
+}
+
+extern "C" int nufft3d_profile(nufft3d_plan *p, int enable)
+{
+    clear_error();
+    if (!p) return fail(NUFFT3D_ERR_ARG, "plan is NULL");
+    DevGuard g(p->device);
+    NUFFT_TRY(profile_resolve(p));
+    Profiler &pr = p->prof;
+    for (int i = 0; i < ST_COUNT; ++i) {
+        pr.ms[i] = 0;
+        pr.launches[i] = 0;
+        pr.calls[i] = 0;
+    }
+    pr.on = enable != 0;
+    return NUFFT3D_SUCCESS;
+}
+
+extern "C" int nufft3d_profile_read(nufft3d_plan *p, char *buf, int cap)
+{
+    clear_error();
+    if (!p || !buf || cap <= 0) return fail(NUFFT3D_ERR_ARG, "NULL argument");
+    DevGuard g(p->device);
+    NUFFT_TRY(profile_resolve(p));
+    std::string out = "{";
+    const Profiler &pr = p->prof;
+    bool first = true;
+    for (int i = 0; i < ST_COUNT; ++i) {
+        if (!pr.calls[i]) continue;
+        char tmp[256];
+        std::snprintf(tmp, sizeof tmp, "%s\"%s\": {\"calls\": %lld, \"launches\": %lld, \"ms\": %.6f}",
+                      first ? "" : ", ", kStageNames[i], pr.calls[i], pr.launches[i], pr.ms[i]);
+        out += tmp;
+        first = false;
+    }
+    out += "}";
+    if ((int)out.size() + 1 > cap) return fail(NUFFT3D_ERR_SIZE, "profile buffer too small");
+    std::memcpy(buf, out.c_str(), out.size() + 1);
     return NUFFT3D_SUCCESS;
 }

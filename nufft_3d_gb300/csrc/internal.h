@@ -44,10 +44,25 @@ struct KBParams {
     float half2;        // (J/2)^2: tap kept iff dist2 <= half2 (4*dist2 <= J^2)
 };
 
+// exp(x) for x <= 0 by Cody-Waite range reduction: x*log2(e) = hi + lo with
+// hi = rn(x*L2E) and lo its rounding residual (exact by FMA) plus the tail of
+// log2(e); 2^hi comes from ex2.approx and 2^lo ~ 1 + lo*ln2 (|lo| <= 2^-24*|hi|).
+__device__ __forceinline__ float exp_neg(float x)
+{
+    const float L2E = 1.44269504088896341f;
+    const float L2E_LO = 1.925963033500e-8f;   // log2(e) - L2E
+    const float hi = x * L2E;
+    const float lo = fmaf(x, L2E, -hi) + x * L2E_LO;
+    float e;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(e) : "f"(hi));
+    return fmaf(e, lo * 0.69314718055994531f, e);
+}
+
 __device__ __forceinline__ float kb_weight(float dist2, const KBParams &p)
 {
-    float t = fmaxf(fmaf(-dist2, p.inv_half2, 1.0f), 0.0f);
-    float y = p.a2_over * t; // (ax/3.75)^2
+    // (J/2)^2 - dist2 is exact for dist2 in [(J/2)^2/2, (J/2)^2] (Sterbenz)
+    const float t = fmaxf((p.half2 - dist2) * p.inv_half2, 0.0f);
+    const float y = p.a2_over * t; // (ax/3.75)^2
     if (y < 1.0f) {
         float s = fmaf(y, 0.45813e-2f, 0.360768e-1f);
         s = fmaf(y, s, 0.2659732f);
@@ -57,8 +72,10 @@ __device__ __forceinline__ float kb_weight(float dist2, const KBParams &p)
         s = fmaf(y, s, 1.0f);
         return s * p.inv_i0a;
     }
-    float ax = p.alpha * sqrtf(t);
-    float z = 3.75f / ax;
+    // large branch: t >= 3.75^2/alpha^2 > 0, so the rsqrt forms are exact enough
+    const float ax = p.alpha * (t * rsqrtf(t));  // alpha*sqrt(t)
+    const float ra = rsqrtf(ax);                 // ax^(-1/2)
+    const float z = 3.75f * (ra * ra);           // 3.75/ax
     float s = fmaf(z, 0.392377e-2f, -0.1647633e-1f);
     s = fmaf(z, s, 0.2635537e-1f);
     s = fmaf(z, s, -0.2057706e-1f);
@@ -67,7 +84,7 @@ __device__ __forceinline__ float kb_weight(float dist2, const KBParams &p)
     s = fmaf(z, s, 0.225319e-2f);
     s = fmaf(z, s, 0.1328592e-1f);
     s = fmaf(z, s, 0.39894228f);
-    return expf(ax - p.alpha) * rsqrtf(ax) * s * p.exp_over_i0a;
+    return exp_neg(ax - p.alpha) * ra * s * p.exp_over_i0a;
 }
 
 // ------------------------------------------------------------ geometry
@@ -110,6 +127,28 @@ struct HostStage {
     float *in = nullptr, *out = nullptr;   // device staging for host-pointer calls
 };
 
+// Per-stage CUDA-event timing (nufft3d_profile): events are recorded on the
+// launching stream around each stage and resolved when read.
+enum Stage {
+    ST_FFT_X_FWD, ST_FFT_Y_FWD, ST_FFT_Z_FWD, ST_GATHER, ST_PERMUTE_OUT, ST_PERMUTE_IN,
+    ST_GRID_ZERO, ST_SPREAD, ST_FFT_Z_ADJ, ST_FFT_Y_ADJ, ST_FFT_X_ADJ, ST_COUNT
+};
+extern const char *const kStageNames[ST_COUNT];
+
+struct Profiler {
+    bool on = false;
+    struct Rec {
+        int stage;
+        int launches;
+        cudaEvent_t a, b;
+    };
+    std::vector<Rec> pending;
+    std::vector<cudaEvent_t> pool;
+    double ms[ST_COUNT] = {0};
+    long long launches[ST_COUNT] = {0};
+    long long calls[ST_COUNT] = {0};
+};
+
 struct SolverWork {
     int nc = 0;
     size_t nimg = 0;
@@ -135,7 +174,9 @@ struct nufft3d_plan {
     float4 *samples = nullptr;  // (fx, fy, fz, packed local coords), sorted by tile
     int32_t *perm = nullptr;    // sorted -> original
     int32_t *inv = nullptr;     // original -> sorted, -1 out of bounds
-    int4 *blocks = nullptr;     // (tile, start, count, 0)
+    int4 *blocks = nullptr;     // (tile, start, count, float bits of max summed weight)
+    int *cand = nullptr;        // candidate tap offsets (reflected octant), packed
+    int n_cand = 0;
     int64_t n_blocks = 0;
     int coils_per_pass = 8;
     int threads = 256;
@@ -151,6 +192,7 @@ struct nufft3d_plan {
     float *wbuf = nullptr;      // sorted sample weights for iNUFT (W.*d)
     int64_t table_bytes = 0;
     cudaStream_t own_stream = nullptr;
+    nufft3d::Profiler prof;
 };
 
 namespace nufft3d {
@@ -169,6 +211,8 @@ int launch_ix(nufft3d_plan *p, const float2 *B1, float2 *img, int nc, float scal
 // gather: ks[s*nc + c] = scale * w_s * sum_taps w * G[...]  (wsample may be null)
 int launch_gather(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, float scale,
                   const float *wsample, cudaStream_t s);
+// plan time: per-block bound on summed weights (blocks[b].w) for the spread
+int launch_weight_sum(nufft3d_plan *p, cudaStream_t s);
 // spread: G += H' ks (G zeroed by caller)
 int launch_spread(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, cudaStream_t s);
 // user [M nc] <-> sorted [nnz][nc]
@@ -196,6 +240,22 @@ int run_inverse(nufft3d_plan *p, const float2 *raw, float2 *x, int nc, int maxit
                 cudaStream_t s);
 
 size_t smem_interp_bytes(const Geom &g, int cb);
+size_t cand_smem_bytes(int n);
+
+// Stage timing scope: records an event pair on stream s when profiling is on
+// (and the stream is not being captured into a graph).
+struct StageTimer {
+    nufft3d_plan *p;
+    int stage;
+    int launches;
+    cudaStream_t s;
+    cudaEvent_t a = nullptr;
+    StageTimer(nufft3d_plan *p_, int stage_, int launches_, cudaStream_t s_);
+    ~StageTimer();
+};
+int coil_passes(const nufft3d_plan *p, int nc);
+int profile_resolve(nufft3d_plan *p);
+void profile_release(nufft3d_plan *p);
 int configure_kernels();
 
 } // namespace nufft3d

@@ -22,7 +22,8 @@
 
 namespace nufft3d {
 
-constexpr int kInterpThreads = 256;
+constexpr int kInterpThreads = 1024;
+constexpr int kGroup = 8;                 // lanes sharing one sample
 
 __device__ __forceinline__ int wrap_idx(int x, int K)
 {
@@ -30,166 +31,379 @@ __device__ __forceinline__ int wrap_idx(int x, int K)
     return x < 0 ? x + K : x;
 }
 
-// Visit the taps of one sample: BODY sees `w` (weight) and `tp` (offset of
-// the tap in the padded tile, in grid points).
-template <int R, bool RADIAL, int RZ, typename F>
-__device__ __forceinline__ void for_taps(const float4 rec, int Px, int Py, const KBParams &kb,
-                                         F &&body)
+// Candidate tap offsets, reflected into the octant f >= 0: packed
+// (dx+8) | (dy+8)<<4 | (dz+8)<<8, sorted so taps kept for every f come first.
+// A sample with fractional offset f uses offset s*d' where s = sign(f) per
+// axis and tests (d' - |f|)^2 per axis -- the same value as (s*d' - f)^2.
+struct Cand {
+    const int *list;
+    int n;
+};
+
+// Per-block candidate tables in shared memory: offsets as floats for the
+// distance test and the tile offset of each candidate in each of the 8 sign
+// octants.
+struct CandSmem {
+    float4 *f;  // [n] (dx', dy', dz', 0)
+    int *off;   // [n][8]
+};
+
+__device__ __forceinline__ void build_cand(const Cand &cd, CandSmem cs, int Px, int PxPy)
 {
-    const int packed = __float_as_int(rec.w);
-    const int lx0 = packed & 0xFF, ly0 = (packed >> 8) & 0xFF, lz0 = (packed >> 16) & 0xFF;
-    const float h2 = kb.half2;
-    float wxs[2 * R + 1];
-    if (!RADIAL) {
+    for (int i = threadIdx.x; i < cd.n; i += blockDim.x) {
+        const int code = cd.list[i];
+        const int dx = (code & 15) - 8, dy = ((code >> 4) & 15) - 8, dz = ((code >> 8) & 15) - 8;
+        cs.f[i] = make_float4((float)dx, (float)dy, (float)dz, 0.f);
 #pragma unroll
-        for (int dx = -R; dx <= R; ++dx) {
-            const float ex = dx - rec.x;
-            const float ex2 = ex * ex;
-            wxs[dx + R] = ex2 <= h2 ? kb_weight(ex2, kb) : 0.f;
+        for (int o = 0; o < 8; ++o) {
+            const int sx = (o & 1) ? -1 : 1, sy = (o & 2) ? -1 : 1, sz = (o & 4) ? -1 : 1;
+            cs.off[i * 8 + o] = sz * dz * PxPy + sy * dy * Px + sx * dx;
         }
     }
-#pragma unroll 1
-    for (int dz = -RZ; dz <= RZ; ++dz) {
-        const float ez = dz - rec.z;
-        const float ez2 = ez * ez;
-        if (ez2 > h2) continue;
-        const float wz = RADIAL ? 1.f : kb_weight(ez2, kb);
-#pragma unroll 1
-        for (int dy = -R; dy <= R; ++dy) {
-            const float ey = dy - rec.y;
-            const float ey2 = ey * ey;
-            const float eyz2 = RADIAL ? ez2 + ey2 : ey2;
-            if (eyz2 > h2) continue;
-            const float wyz = RADIAL ? 1.f : wz * kb_weight(ey2, kb);
-            const int rowoff = ((lz0 + dz) * Py + (ly0 + dy)) * Px + lx0;
+}
+
+size_t cand_smem_bytes(int n) { return (size_t)n * (sizeof(float4) + 8 * sizeof(int)); }
+
+// Per-sample reflected coordinates.
+struct SampleGeo {
+    float fx, fy, fz;  // |f|
+    int oct;           // sign octant: bit0 x<0, bit1 y<0, bit2 z<0
+    int base;          // tile-local index of the rounded position
+};
+
+__device__ __forceinline__ SampleGeo sample_geo(const float4 rec, int Px, int Py)
+{
+    SampleGeo g;
+    const int packed = __float_as_int(rec.w);
+    const int lx0 = packed & 0xFF, ly0 = (packed >> 8) & 0xFF, lz0 = (packed >> 16) & 0xFF;
+    g.oct = (rec.x < 0.f ? 1 : 0) | (rec.y < 0.f ? 2 : 0) | (rec.z < 0.f ? 4 : 0);
+    g.fx = fabsf(rec.x);
+    g.fy = fabsf(rec.y);
+    g.fz = fabsf(rec.z);
+    g.base = (lz0 * Py + ly0) * Px + lx0;
+    return g;
+}
+
+// Weight and tile offset of candidate ci for a sample; false outside the
+// kernel support (the neighbour test of nufft_3d.m:183-192).
+template <bool RADIAL>
+__device__ __forceinline__ bool tap(int ci, const SampleGeo &g, const CandSmem &cs, const KBParams &kb,
+                                    float &w, int &off)
+{
+    const float4 cf = cs.f[ci];
+    const float ex = cf.x - g.fx, ey = cf.y - g.fy, ez = cf.z - g.fz;
+    const float ex2 = ex * ex, ey2 = ey * ey, ez2 = ez * ez;
+    const float h2 = kb.half2;
+    if (RADIAL) {
+        const float d2 = ez2 + ey2 + ex2;
+        if (!(d2 <= h2)) return false;
+        w = kb_weight(d2, kb);
+    } else {
+        if (!(ex2 <= h2 && ey2 <= h2 && ez2 <= h2)) return false;
+        w = kb_weight(ez2, kb) * kb_weight(ey2, kb) * kb_weight(ex2, kb);
+    }
+    off = g.base + cs.off[ci * 8 + g.oct];
+    return true;
+}
+
+// Visit every (tile point, coil) of the padded tile with the grid point it
+// maps to: warps take tile rows (one division per row), lanes run along x and
+// the coil index (V values per point) so global accesses stay contiguous.
+// F(pt, c, gidx) with pt the tile-local point and gidx the grid point.
+template <int V, typename F>
+__device__ __forceinline__ void for_tile_rows(const Geom &g, int ox, int oy, int oz, F &&f)
+{
+    const int Px = g.P[0], Py = g.P[1], Pz = g.P[2];
+    const int rowlen = Px * V;
+    const int warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5, lane = threadIdx.x & 31;
+    const bool simple = Px <= g.K[0];
+    for (int row = warp; row < Py * Pz; row += nwarps) {
+        const int ly = row % Py, lz = row / Py;
+        const int gy = wrap_idx(oy + ly, g.K[1]), gz = wrap_idx(oz + lz, g.K[2]);
+        const size_t rb = ((size_t)gz * g.K[1] + gy) * g.K[0];
+        for (int q = lane; q < rowlen; q += 32) {
+            const int lx = q / V, c = q - lx * V;
+            int gx = ox + lx;
+            if (simple) {
+                gx += gx < 0 ? g.K[0] : 0;
+                gx -= gx >= g.K[0] ? g.K[0] : 0;
+            } else {
+                gx = wrap_idx(gx, g.K[0]);
+            }
+            f(row * Px + lx, c, rb + gx);
+        }
+    }
+}
+
+// Gather: tile staged coil-major ([CB][P^3] complex) -> ks.  kGroup lanes per
+// sample walk the candidate list; partial sums are reduced across the group.
+template <int CB, bool RADIAL>
+__global__ void __launch_bounds__(kInterpThreads)
+k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
+         const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
+         KBParams kb, float scale, const float *__restrict__ wsample, Cand cd)
+{
+    extern __shared__ float4 smem4[];
+    const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
+    const int pv = PxPy * g.P[2];
+    CandSmem cs;
+    cs.f = smem4;
+    cs.off = reinterpret_cast<int *>(smem4 + cd.n);
+    float2 *tile = reinterpret_cast<float2 *>(cs.off + 8 * cd.n);
+    const int4 bi = blocks[blockIdx.x];
+    const int tid = bi.x;
+    const int tx = tid % g.nt[0];
+    const int ty = (tid / g.nt[0]) % g.nt[1];
+    const int tz = tid / (g.nt[0] * g.nt[1]);
+    const int ox = tx * g.T[0] - g.Ra[0], oy = ty * g.T[1] - g.Ra[1], oz = tz * g.T[2] - g.Ra[2];
+    const int cb = min(CB, nc - c0);
+    build_cand(cd, cs, Px, PxPy);
+    for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int c, size_t gidx) {
+        tile[c * pv + pt] = c < cb ? G[gidx * nc + c0 + c] : make_float2(0.f, 0.f);
+    });
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int lig = lane & (kGroup - 1);
+    const unsigned gmask = 0xFFu << (lane & ~(kGroup - 1));
+    const int grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
+    const int niter = (cd.n + kGroup - 1) / kGroup;
+    const int send = bi.y + bi.z;
+    float4 rec_next = bi.y + grp < send ? __ldg(&samples[bi.y + grp]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int s = bi.y + grp; s < send; s += ngrp) {
+        const SampleGeo sg = sample_geo(rec_next, Px, g.P[1]);
+        if (s + ngrp < send) rec_next = __ldg(&samples[s + ngrp]);
+        float2 acc[CB];
 #pragma unroll
-            for (int dx = -R; dx <= R; ++dx) {
-                const float ex = dx - rec.x;
-                if (RADIAL) {
-                    const float d2 = fmaf(ex, ex, eyz2);
-                    if (d2 <= h2) body(kb_weight(d2, kb), rowoff + dx);
-                } else {
-                    if (ex * ex <= h2) body(wyz * wxs[dx + R], rowoff + dx);
+        for (int c = 0; c < CB; ++c) acc[c] = make_float2(0.f, 0.f);
+        // two independent candidates per step (ILP)
+        for (int it = 0; it < niter; it += 2) {
+            const int ci0 = it * kGroup + lig, ci1 = ci0 + kGroup;
+            float w0, w1;
+            int off0, off1;
+            const bool h0 = ci0 < cd.n && tap<RADIAL>(ci0, sg, cs, kb, w0, off0);
+            const bool h1 = ci1 < cd.n && tap<RADIAL>(ci1, sg, cs, kb, w1, off1);
+            if (h0) {
+#pragma unroll
+                for (int c = 0; c < CB; ++c) {
+                    const float2 v = tile[c * pv + off0];
+                    acc[c].x = fmaf(w0, v.x, acc[c].x);
+                    acc[c].y = fmaf(w0, v.y, acc[c].y);
+                }
+            }
+            if (h1) {
+#pragma unroll
+                for (int c = 0; c < CB; ++c) {
+                    const float2 v = tile[c * pv + off1];
+                    acc[c].x = fmaf(w1, v.x, acc[c].x);
+                    acc[c].y = fmaf(w1, v.y, acc[c].y);
+                }
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+#pragma unroll
+            for (int o = kGroup / 2; o > 0; o >>= 1) {
+                acc[c].x += __shfl_xor_sync(gmask, acc[c].x, o);
+                acc[c].y += __shfl_xor_sync(gmask, acc[c].y, o);
+            }
+        }
+        const float sc_ = wsample ? scale * __ldg(&wsample[s]) : scale;
+        float2 *o = ks + (size_t)s * nc + c0;
+#pragma unroll
+        for (int c = 0; c < CB; ++c)
+            if (c % kGroup == lig && c < cb) o[c] = make_float2(acc[c].x * sc_, acc[c].y * sc_);
+    }
+}
+
+// Spread: ks -> tile -> grid.  The tile accumulates in 32-bit fixed point
+// with native shared-memory integer reductions (floating-point shared atomics
+// are several times slower on this part).  Per block and call the scale is a
+// power of two 2^F chosen from the largest |Re|,|Im| of the block's samples
+// and the plan-time bound wsum = max over tile points of the summed weights,
+// so that every partial sum stays below 2^30 and every product w*y*2^F below
+// 2^22; products are rounded to integers exactly by the 1.5*2^23 addition.
+// Layout [CB][2][P^3] int32 (split real/imaginary planes, so a warp's
+// scattered taps spread over all banks).  Lanes of a group touch distinct
+// taps; the groups of a warp start on different candidate shells.  The tile
+// is then added to the grid with vector atomics (neighbouring tiles' halos
+// overlap).
+__device__ __forceinline__ float block_max(float v, float *red)
+{
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        float r = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) r = fmaxf(r, __shfl_xor_sync(0xffffffffu, r, o));
+        if (threadIdx.x == 0) red[32] = r;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+__device__ __forceinline__ void red_add(int *p, int v)
+{
+    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+
+// q = round(v) for |v| < 2^22 (exact: the addition rounds to an integer)
+__device__ __forceinline__ int to_fixed(float v)
+{
+    return __float_as_int(v + 12582912.0f) - 0x4B400000;
+}
+
+template <int CB, bool RADIAL>
+__global__ void __launch_bounds__(kInterpThreads)
+k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
+         const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
+         KBParams kb, Cand cd)
+{
+    extern __shared__ float4 smem4[];
+    __shared__ float red[33];
+    const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
+    const int pv = PxPy * g.P[2];
+    CandSmem cs;
+    cs.f = smem4;
+    cs.off = reinterpret_cast<int *>(smem4 + cd.n);
+    int *tile = cs.off + 8 * cd.n;
+    const int4 bi = blocks[blockIdx.x];
+    const int tid = bi.x;
+    const int tx = tid % g.nt[0];
+    const int ty = (tid / g.nt[0]) % g.nt[1];
+    const int tz = tid / (g.nt[0] * g.nt[1]);
+    const int cb = min(CB, nc - c0);
+    const int send = bi.y + bi.z;
+    // scale from the block's largest component
+    float m = 0.f;
+    for (int s = bi.y + threadIdx.x; s < send; s += blockDim.x) {
+        const float2 *src = ks + (size_t)s * nc + c0;
+        for (int c = 0; c < cb; ++c) {
+            const float2 v = src[c];
+            m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+        }
+    }
+    for (int t = threadIdx.x; t < pv * CB * 2; t += blockDim.x) tile[t] = 0;
+    build_cand(cd, cs, Px, PxPy);
+    const float ymax = block_max(m, red);   // contains __syncthreads
+    if (!(ymax > 0.f)) return;             // nothing to add (block-uniform)
+    const float wsum = fmaxf(__int_as_float(bi.w), 1.0f);
+    int ey, ecy;
+    frexpf(ymax, &ey);                     // ymax < 2^ey
+    frexpf(ymax * wsum, &ecy);             // wsum*ymax < 2^ecy
+    const int F = min(22 - ey, 30 - ecy);
+    const float scale = ldexpf(1.f, F), inv_scale = ldexpf(1.f, -F);
+    const int lane = threadIdx.x & 31;
+    const int lig = lane & (kGroup - 1);
+    const int grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
+    const int niter = (cd.n + kGroup - 1) / kGroup;
+    const int rot = ((lane / kGroup) * niter) / (32 / kGroup);
+    float4 rec_next = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 y_next[CB];
+    auto fetch = [&](int s) {
+        rec_next = __ldg(&samples[s]);
+        const float2 *src = ks + (size_t)s * nc + c0;
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+            const float2 v = c < cb ? src[c] : make_float2(0.f, 0.f);
+            y_next[c] = make_float2(v.x * scale, v.y * scale);
+        }
+    };
+    if (bi.y + grp < send) fetch(bi.y + grp);
+    for (int s = bi.y + grp; s < send; s += ngrp) {
+        const SampleGeo sg = sample_geo(rec_next, Px, g.P[1]);
+        float2 yv[CB];
+#pragma unroll
+        for (int c = 0; c < CB; ++c) yv[c] = y_next[c];
+        if (s + ngrp < send) fetch(s + ngrp);
+        for (int it0 = 0; it0 < niter; it0 += 2) {
+            int ita = it0 + rot, itb = it0 + 1 + rot;
+            if (ita >= niter) ita -= niter;
+            if (itb >= niter) itb -= niter;
+            const int ci0 = ita * kGroup + lig, ci1 = itb * kGroup + lig;
+            float w0, w1;
+            int off0, off1;
+            const bool h0 = ci0 < cd.n && tap<RADIAL>(ci0, sg, cs, kb, w0, off0);
+            const bool h1 = it0 + 1 < niter && ci1 < cd.n && tap<RADIAL>(ci1, sg, cs, kb, w1, off1);
+            if (h0) {
+#pragma unroll
+                for (int c = 0; c < CB; ++c) {
+                    red_add(&tile[(2 * c) * pv + off0], to_fixed(w0 * yv[c].x));
+                    red_add(&tile[(2 * c + 1) * pv + off0], to_fixed(w0 * yv[c].y));
+                }
+            }
+            if (h1) {
+#pragma unroll
+                for (int c = 0; c < CB; ++c) {
+                    red_add(&tile[(2 * c) * pv + off1], to_fixed(w1 * yv[c].x));
+                    red_add(&tile[(2 * c + 1) * pv + off1], to_fixed(w1 * yv[c].y));
                 }
             }
         }
     }
-}
-
-template <int CB>
-__device__ __forceinline__ void stage_tile(float2 *tile, const float2 *__restrict__ G, int nc,
-                                           int c0, int cb, const Geom &g, int ox, int oy, int oz)
-{
-    const int Px = g.P[0], Py = g.P[1], Pz = g.P[2];
-    const int n = Px * Py * Pz * CB;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        const int c = t % CB;
-        const int pt = t / CB;
-        const int lx = pt % Px;
-        const int r = pt / Px;
-        const int ly = r % Py;
-        const int lz = r / Py;
-        float2 v = make_float2(0.f, 0.f);
-        if (c < cb) {
-            const int gx = wrap_idx(ox + lx, g.K[0]);
-            const int gy = wrap_idx(oy + ly, g.K[1]);
-            const int gz = wrap_idx(oz + lz, g.K[2]);
-            v = G[(((size_t)gz * g.K[1] + gy) * g.K[0] + gx) * nc + c0 + c];
-        }
-        tile[t] = v;
-    }
-}
-
-template <int CB, int R, bool RADIAL, int RZ>
-__global__ void __launch_bounds__(kInterpThreads)
-k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
-         const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
-         KBParams kb, float scale, const float *__restrict__ wsample)
-{
-    extern __shared__ float2 tile[];
-    const int4 bi = blocks[blockIdx.x];
-    const int tid = bi.x;
-    const int tx = tid % g.nt[0];
-    const int ty = (tid / g.nt[0]) % g.nt[1];
-    const int tz = tid / (g.nt[0] * g.nt[1]);
-    const int cb = min(CB, nc - c0);
-    stage_tile<CB>(tile, G, nc, c0, cb, g, tx * g.T[0] - g.Ra[0], ty * g.T[1] - g.Ra[1],
-                   tz * g.T[2] - g.Ra[2]);
-    __syncthreads();
-    const int Px = g.P[0], Py = g.P[1];
-    for (int s = bi.y + threadIdx.x; s < bi.y + bi.z; s += blockDim.x) {
-        const float4 rec = __ldg(&samples[s]);
-        float2 acc[CB];
-#pragma unroll
-        for (int c = 0; c < CB; ++c) acc[c] = make_float2(0.f, 0.f);
-        for_taps<R, RADIAL, RZ>(rec, Px, Py, kb, [&](float w, int off) {
-            const float2 *tp = tile + (size_t)off * CB;
-#pragma unroll
-            for (int c = 0; c < CB; ++c) {
-                const float2 v = tp[c];
-                acc[c].x = fmaf(w, v.x, acc[c].x);
-                acc[c].y = fmaf(w, v.y, acc[c].y);
-            }
-        });
-        const float sc = wsample ? scale * __ldg(&wsample[s]) : scale;
-        float2 *o = ks + (size_t)s * nc + c0;
-#pragma unroll
-        for (int c = 0; c < CB; ++c)
-            if (c < cb) o[c] = make_float2(acc[c].x * sc, acc[c].y * sc);
-    }
-}
-
-template <int CB, int R, bool RADIAL, int RZ>
-__global__ void __launch_bounds__(kInterpThreads)
-k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
-         const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
-         KBParams kb)
-{
-    extern __shared__ float2 tile[];
-    const int4 bi = blocks[blockIdx.x];
-    const int tid = bi.x;
-    const int tx = tid % g.nt[0];
-    const int ty = (tid / g.nt[0]) % g.nt[1];
-    const int tz = tid / (g.nt[0] * g.nt[1]);
-    const int cb = min(CB, nc - c0);
-    const int Px = g.P[0], Py = g.P[1], Pz = g.P[2];
-    const int n = Px * Py * Pz * CB;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) tile[t] = make_float2(0.f, 0.f);
-    __syncthreads();
-    for (int s = bi.y + threadIdx.x; s < bi.y + bi.z; s += blockDim.x) {
-        const float4 rec = __ldg(&samples[s]);
-        float2 yv[CB];
-        const float2 *src = ks + (size_t)s * nc + c0;
-#pragma unroll
-        for (int c = 0; c < CB; ++c) yv[c] = c < cb ? src[c] : make_float2(0.f, 0.f);
-        for_taps<R, RADIAL, RZ>(rec, Px, Py, kb, [&](float w, int off) {
-            float2 *tp = tile + (size_t)off * CB;
-#pragma unroll
-            for (int c = 0; c < CB; ++c) {
-                atomicAdd(&tp[c].x, w * yv[c].x);
-                atomicAdd(&tp[c].y, w * yv[c].y);
-            }
-        });
-    }
     __syncthreads();
     const int ox = tx * g.T[0] - g.Ra[0], oy = ty * g.T[1] - g.Ra[1], oz = tz * g.T[2] - g.Ra[2];
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        const int c = t % CB;
-        if (c >= cb) continue;
-        const float2 v = tile[t];
-        if (v.x == 0.f && v.y == 0.f) continue;
-        const int pt = t / CB;
-        const int lx = pt % Px;
-        const int r = pt / Px;
-        const int ly = r % Py;
-        const int lz = r / Py;
-        const int gx = wrap_idx(ox + lx, g.K[0]);
-        const int gy = wrap_idx(oy + ly, g.K[1]);
-        const int gz = wrap_idx(oz + lz, g.K[2]);
-        atomicAdd(&G[(((size_t)gz * g.K[1] + gy) * g.K[0] + gx) * nc + c0 + c], v);
+    if (CB % 2 == 0 && nc % 2 == 0 && c0 % 2 == 0) {
+        for_tile_rows<CB / 2>(g, ox, oy, oz, [&](int pt, int cq, size_t gidx) {
+            const int c = 2 * cq;
+            if (c >= cb) return;
+            const int a = tile[(2 * c) * pv + pt], b = tile[(2 * c + 1) * pv + pt];
+            const int e = tile[(2 * c + 2) * pv + pt], f = tile[(2 * c + 3) * pv + pt];
+            if ((a | b | e | f) == 0) return;
+            atomicAdd(reinterpret_cast<float4 *>(&G[gidx * nc + c0 + c]),
+                      make_float4(a * inv_scale, b * inv_scale, e * inv_scale, f * inv_scale));
+        });
+    } else {
+        for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int c, size_t gidx) {
+            if (c >= cb) return;
+            const int a = tile[(2 * c) * pv + pt], b = tile[(2 * c + 1) * pv + pt];
+            if ((a | b) == 0) return;
+            atomicAdd(&G[gidx * nc + c0 + c], make_float2(a * inv_scale, b * inv_scale));
+        });
     }
 }
 
+// Plan-time bound for the fixed-point spread: for each block, the largest
+// sum of kernel weights its samples put on one tile point (float shared
+// atomics; runs once per plan).  Written to blocks[b].w as float bits.
+template <bool RADIAL>
+__global__ void __launch_bounds__(kInterpThreads)
+k_weight_sum(const float4 *__restrict__ samples, int4 *__restrict__ blocks, Geom g, KBParams kb, Cand cd)
+{
+    extern __shared__ float4 smem4[];
+    __shared__ float red[33];
+    const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
+    const int pv = PxPy * g.P[2];
+    CandSmem cs;
+    cs.f = smem4;
+    cs.off = reinterpret_cast<int *>(smem4 + cd.n);
+    float *tile = reinterpret_cast<float *>(cs.off + 8 * cd.n);
+    const int4 bi = blocks[blockIdx.x];
+    for (int t = threadIdx.x; t < pv; t += blockDim.x) tile[t] = 0.f;
+    build_cand(cd, cs, Px, PxPy);
+    __syncthreads();
+    const int lig = threadIdx.x & (kGroup - 1);
+    const int grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
+    const int niter = (cd.n + kGroup - 1) / kGroup;
+    for (int s = bi.y + grp; s < bi.y + bi.z; s += ngrp) {
+        const SampleGeo sg = sample_geo(__ldg(&samples[s]), Px, g.P[1]);
+        for (int it = 0; it < niter; ++it) {
+            const int ci = it * kGroup + lig;
+            float w;
+            int off;
+            if (ci < cd.n && tap<RADIAL>(ci, sg, cs, kb, w, off)) atomicAdd(&tile[off], w);
+        }
+    }
+    __syncthreads();
+    float m = 0.f;
+    for (int t = threadIdx.x; t < pv; t += blockDim.x) m = fmaxf(m, tile[t]);
+    m = block_max(m, red);
+    // small safety margin over the single-precision sums
+    if (threadIdx.x == 0) blocks[blockIdx.x].w = __float_as_int(m * 1.001f + 1e-3f);
+}
+
+// user layout [M][nc] (coil-major) <-> sorted [nnz][nc] (coil fastest); the
+// sorted side is read/written as one contiguous nc-vector per sample.
 __global__ void k_permute_out(const float2 *__restrict__ ks, float2 *__restrict__ k,
                               const int32_t *__restrict__ inv, int64_t M, int nc, float scale)
 {
@@ -228,57 +442,37 @@ size_t smem_interp_bytes(const Geom &g, int cb)
     return (size_t)g.P[0] * g.P[1] * g.P[2] * cb * sizeof(float2);
 }
 
-template <int CB, int R, bool RADIAL, int RZ>
+static Cand cand_of(const nufft3d_plan *p) { return Cand{p->cand, p->n_cand}; }
+
+template <int CB, bool RADIAL>
 static int gather_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, int c0, float scale,
                     const float *ws, cudaStream_t s)
 {
-    const size_t smem = smem_interp_bytes(p->geom, CB);
-    k_gather<CB, R, RADIAL, RZ><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
-        G, ks, nc, c0, p->samples, p->blocks, p->geom, p->kb, scale, ws);
+    const size_t smem = smem_interp_bytes(p->geom, CB) + cand_smem_bytes(p->n_cand);
+    k_gather<CB, RADIAL><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
+        G, ks, nc, c0, p->samples, p->blocks, p->geom, p->kb, scale, ws, cand_of(p));
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }
 
-template <int CB, int R, bool RADIAL, int RZ>
+template <int CB, bool RADIAL>
 static int spread_t(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, int c0, cudaStream_t s)
 {
-    const size_t smem = smem_interp_bytes(p->geom, CB);
-    k_spread<CB, R, RADIAL, RZ><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
-        ks, G, nc, c0, p->samples, p->blocks, p->geom, p->kb);
+    const size_t smem = smem_interp_bytes(p->geom, CB) + cand_smem_bytes(p->n_cand);
+    k_spread<CB, RADIAL><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
+        ks, G, nc, c0, p->samples, p->blocks, p->geom, p->kb, cand_of(p));
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
-}
-
-// Dispatch over (coils per pass, R, radial, 2D).
-template <bool GATHER, int CB, int R>
-static int dispatch_rz(nufft3d_plan *p, const float2 *in, float2 *out, int nc, int c0, float scale,
-                       const float *ws, cudaStream_t s)
-{
-    const bool rad = p->geom.radial != 0;
-    const bool flat = p->geom.is2d != 0;
-    if (GATHER) {
-        if (rad) return flat ? gather_t<CB, R, true, 0>(p, in, out, nc, c0, scale, ws, s)
-                             : gather_t<CB, R, true, R>(p, in, out, nc, c0, scale, ws, s);
-        return flat ? gather_t<CB, R, false, 0>(p, in, out, nc, c0, scale, ws, s)
-                    : gather_t<CB, R, false, R>(p, in, out, nc, c0, scale, ws, s);
-    }
-    if (rad) return flat ? spread_t<CB, R, true, 0>(p, in, out, nc, c0, s)
-                         : spread_t<CB, R, true, R>(p, in, out, nc, c0, s);
-    return flat ? spread_t<CB, R, false, 0>(p, in, out, nc, c0, s)
-                : spread_t<CB, R, false, R>(p, in, out, nc, c0, s);
 }
 
 template <bool GATHER, int CB>
-static int dispatch_r(nufft3d_plan *p, const float2 *in, float2 *out, int nc, int c0, float scale,
-                      const float *ws, cudaStream_t s)
+static int dispatch(nufft3d_plan *p, const float2 *in, float2 *out, int nc, int c0, float scale,
+                    const float *ws, cudaStream_t s)
 {
-    switch (p->geom.R) {
-    case 1: return dispatch_rz<GATHER, CB, 1>(p, in, out, nc, c0, scale, ws, s);
-    case 2: return dispatch_rz<GATHER, CB, 2>(p, in, out, nc, c0, scale, ws, s);
-    case 3: return dispatch_rz<GATHER, CB, 3>(p, in, out, nc, c0, scale, ws, s);
-    case 4: return dispatch_rz<GATHER, CB, 4>(p, in, out, nc, c0, scale, ws, s);
-    default: return fail(NUFFT3D_ERR_UNSUPPORTED, "kernel half-width ceil(J/2) must be 1..4");
-    }
+    const bool rad = p->geom.radial != 0;
+    if (GATHER) return rad ? gather_t<CB, true>(p, in, out, nc, c0, scale, ws, s)
+                           : gather_t<CB, false>(p, in, out, nc, c0, scale, ws, s);
+    return rad ? spread_t<CB, true>(p, in, out, nc, c0, s) : spread_t<CB, false>(p, in, out, nc, c0, s);
 }
 
 template <bool GATHER>
@@ -293,14 +487,28 @@ static int interp(nufft3d_plan *p, const float2 *in, float2 *out, int nc, float 
         while (cb < rem && cb < cmax) cb *= 2;
         int st;
         switch (cb) {
-        case 1: st = dispatch_r<GATHER, 1>(p, in, out, nc, c0, scale, ws, s); break;
-        case 2: st = dispatch_r<GATHER, 2>(p, in, out, nc, c0, scale, ws, s); break;
-        case 4: st = dispatch_r<GATHER, 4>(p, in, out, nc, c0, scale, ws, s); break;
-        default: st = dispatch_r<GATHER, 8>(p, in, out, nc, c0, scale, ws, s); break;
+        case 1: st = dispatch<GATHER, 1>(p, in, out, nc, c0, scale, ws, s); break;
+        case 2: st = dispatch<GATHER, 2>(p, in, out, nc, c0, scale, ws, s); break;
+        case 4: st = dispatch<GATHER, 4>(p, in, out, nc, c0, scale, ws, s); break;
+        default: st = dispatch<GATHER, 8>(p, in, out, nc, c0, scale, ws, s); break;
         }
         if (st != NUFFT3D_SUCCESS) return st;
         if (cb > rem) break;
     }
+    return NUFFT3D_SUCCESS;
+}
+
+int launch_weight_sum(nufft3d_plan *p, cudaStream_t s)
+{
+    if (p->n_blocks == 0) return NUFFT3D_SUCCESS;
+    const size_t smem = smem_interp_bytes(p->geom, 1) / 2 + cand_smem_bytes(p->n_cand);
+    if (p->geom.radial)
+        k_weight_sum<true><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(p->samples, p->blocks, p->geom,
+                                                                            p->kb, cand_of(p));
+    else
+        k_weight_sum<false><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(p->samples, p->blocks, p->geom,
+                                                                             p->kb, cand_of(p));
+    NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }
 
@@ -337,44 +545,25 @@ int launch_permute_in(nufft3d_plan *p, const float2 *k, float2 *ks, int nc,
     return NUFFT3D_SUCCESS;
 }
 
-template <bool GATHER, int CB, int R>
-static int cfg_rz()
+template <int CB>
+static int cfg_cb()
 {
-    const int mx = 227 * 1024;
-    if (GATHER) {
-        NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_gather<CB, R, true, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-        NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_gather<CB, R, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-        NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_gather<CB, R, false, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-        NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_gather<CB, R, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    } else {
-        NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_spread<CB, R, true, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-        NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_spread<CB, R, true, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-        NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_spread<CB, R, false, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-        NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_spread<CB, R, false, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    }
-    return NUFFT3D_SUCCESS;
-}
-
-template <bool GATHER, int CB>
-static int cfg_r()
-{
-    NUFFT_TRY((cfg_rz<GATHER, CB, 1>()));
-    NUFFT_TRY((cfg_rz<GATHER, CB, 2>()));
-    NUFFT_TRY((cfg_rz<GATHER, CB, 3>()));
-    NUFFT_TRY((cfg_rz<GATHER, CB, 4>()));
+    const int mx = 227 * 1024 - 2048; // leave room for static shared memory
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_gather<CB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_gather<CB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_spread<CB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_spread<CB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
     return NUFFT3D_SUCCESS;
 }
 
 int configure_interp_kernels()
 {
-    NUFFT_TRY((cfg_r<true, 1>()));
-    NUFFT_TRY((cfg_r<true, 2>()));
-    NUFFT_TRY((cfg_r<true, 4>()));
-    NUFFT_TRY((cfg_r<true, 8>()));
-    NUFFT_TRY((cfg_r<false, 1>()));
-    NUFFT_TRY((cfg_r<false, 2>()));
-    NUFFT_TRY((cfg_r<false, 4>()));
-    NUFFT_TRY((cfg_r<false, 8>()));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_weight_sum<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - 2048));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_weight_sum<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - 2048));
+    NUFFT_TRY(cfg_cb<1>());
+    NUFFT_TRY(cfg_cb<2>());
+    NUFFT_TRY(cfg_cb<4>());
+    NUFFT_TRY(cfg_cb<8>());
     return NUFFT3D_SUCCESS;
 }
 

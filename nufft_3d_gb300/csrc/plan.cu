@@ -138,6 +138,56 @@ static std::vector<double> deap_host(const int N[3], const int K[3], double J, d
     return U;
 }
 
+// Candidate taps for the octant f in [0, 1/2]^3 (samples are reflected onto
+// it): offsets d' in [-R, R]^3 whose smallest possible distance over that
+// octant is inside the support, ordered so that offsets inside the support
+// for every f come first.  A relative slack of 1e-5 keeps every tap that the
+// single-precision test in the kernels can accept.
+static std::vector<int> make_candidates(int R, int radial, int is2d, double J)
+{
+    const double h2 = (J / 2) * (J / 2) * (1 + 1e-5);
+    auto mn = [](int d) { return d <= 0 ? double(d) * d : (d - 0.5) * (d - 0.5); };
+    auto mx = [](int d) { return d >= 0.25 ? double(d) * d : (d - 0.5) * (d - 0.5); };
+    struct C {
+        double key, key2;
+        int code;
+    };
+    std::vector<C> v;
+    const int rz = is2d ? 0 : R;
+    for (int dz = -rz; dz <= rz; ++dz)
+        for (int dy = -R; dy <= R; ++dy)
+            for (int dx = -R; dx <= R; ++dx) {
+                bool keep;
+                double key;
+                if (radial) {
+                    keep = mn(dx) + mn(dy) + mn(dz) <= h2;
+                    key = mx(dx) + mx(dy) + mx(dz);
+                } else {
+                    keep = mn(dx) <= h2 && mn(dy) <= h2 && mn(dz) <= h2;
+                    key = std::max(mx(dx), std::max(mx(dy), mx(dz)));
+                }
+                if (keep) v.push_back({key, mn(dx) + mn(dy) + mn(dz), (dx + 8) | ((dy + 8) << 4) | ((dz + 8) << 8)});
+            }
+    std::stable_sort(v.begin(), v.end(), [](const C &a, const C &b) {
+        return a.key != b.key ? a.key < b.key : a.key2 < b.key2;
+    });
+    // within each chunk of 8 (one iteration of a lane group) order row-major so
+    // the group's lanes touch neighbouring words of the tile (fewer conflicts)
+    for (size_t i = 0; i < v.size(); i += 8) {
+        const size_t e = std::min(v.size(), i + 8);
+        std::sort(v.begin() + i, v.begin() + e, [](const C &a, const C &b) {
+            const int za = a.code >> 8, zb = b.code >> 8;
+            const int ya = (a.code >> 4) & 15, yb = (b.code >> 4) & 15;
+            if (za != zb) return za < zb;
+            if (ya != yb) return ya < yb;
+            return (a.code & 15) < (b.code & 15);
+        });
+    }
+    std::vector<int> out;
+    for (auto &c : v) out.push_back(c.code);
+    return out;
+}
+
 // ------------------------------------------------------ device kernels
 struct KeyParams {
     double u;
@@ -273,6 +323,7 @@ static void free_plan_memory(nufft3d_plan *p)
     F(p->perm);
     F(p->inv);
     F(p->blocks);
+    F(p->cand);
     F(p->U);
     F(p->d);
     F(p->d_orig);
@@ -287,6 +338,7 @@ static void free_plan_memory(nufft3d_plan *p)
     SolverWork &w = p->solver;
     F(w.x); F(w.r); F(w.p); F(w.q); F(w.v); F(w.vprev); F(w.w1); F(w.w2);
     F(w.partial); F(w.scal); F(w.iters);
+    profile_release(p);
     if (p->own_stream) cudaStreamDestroy(p->own_stream);
 }
 
@@ -435,6 +487,14 @@ static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts
         p->taps = (double)ht / (double)nnz;
     }
 
+    {
+        std::vector<int> cand = make_candidates(g.R, g.radial, g.is2d, p->J);
+        if (cand.size() > 512) return fail(NUFFT3D_ERR_UNSUPPORTED, "too many candidate taps");
+        p->n_cand = (int)cand.size();
+        NUFFT_TRY(dmalloc(&p->cand, cand.size(), &p->table_bytes));
+        NUFFT_CUDA_TRY(cudaMemcpyAsync(p->cand, cand.data(), sizeof(int) * cand.size(), cudaMemcpyHostToDevice, s));
+    }
+    NUFFT_TRY(launch_weight_sum(p, s));
     // deapodization (FP64 on the host, stored FP32 like deap.m:100-101)
     {
         std::vector<double> U = deap_host(p->N, g.K, p->J, p->alpha, g.radial, g.is2d);
@@ -597,8 +657,10 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
     int cpp = o.max_coils_per_pass > 0 ? o.max_coils_per_pass : 8;
     int cb = 1;
     while (cb * 2 <= cpp && cb < 8) cb *= 2;
-    while (cb > 1 && smem_interp_bytes(g, cb) > 200 * 1024) cb /= 2;
-    if (smem_interp_bytes(g, cb) > 227 * 1024) {
+    // the kernels also hold the candidate tables (<= 461 taps for R <= 4)
+    const size_t cand_max = cand_smem_bytes(R <= 2 ? 128 : (R == 3 ? 256 : 512));
+    while (cb > 1 && smem_interp_bytes(g, cb) + cand_max > 210 * 1024) cb /= 2;
+    if (smem_interp_bytes(g, cb) + cand_max > 227 * 1024) {
         delete p;
         return fail(NUFFT3D_ERR_UNSUPPORTED, "interpolation tile too large for shared memory");
     }

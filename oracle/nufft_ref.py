@@ -111,7 +111,8 @@ class NufftRef:
     """
 
     def __init__(self, om, N, J=4, u=2, alpha=0, radial=True, d=None,
-                 matrix=True, density_iters=20):
+                 matrix=True, density_iters=20, workers=None):
+        self.workers = workers  # scipy.fft threads (None: numpy.fft)
         om = np.asarray(om)
         if om.ndim < 1 or om.shape[0] != 3 or om.size == 0 or np.iscomplexobj(om):
             raise ValueError("om must be a real array with leading dimension of 3")
@@ -268,14 +269,20 @@ class NufftRef:
             widths = [(0, 0)] * x.ndim
             widths[j] = (pad, pad)
             x = np.pad(x, widths)
-            x = np.fft.fft(np.fft.fftshift(x, axes=j), axis=j)
+            x = self._fft(np.fft.fftshift(x, axes=j), j, inverse=False)
         return x
+
+    def _fft(self, x, axis, inverse):
+        if self.workers:
+            import scipy.fft as sf
+            return (sf.ifft if inverse else sf.fft)(x, axis=axis, workers=self.workers)
+        return (np.fft.ifft if inverse else np.fft.fft)(x, axis=axis)
 
     def ifft3_crop(self, k):
         """nufft_3d.m:294-302."""
         for j in range(3):
             mid = (int(self.K[j]) - int(self.N[j])) // 2
-            k = np.fft.ifftshift(np.fft.ifft(k, axis=j), axes=j) * self.K[j]
+            k = np.fft.ifftshift(self._fft(k, j, inverse=True), axes=j) * self.K[j]
             sl = [slice(None)] * k.ndim
             sl[j] = slice(mid, int(self.K[j]) - mid)
             k = k[tuple(sl)]
