@@ -158,7 +158,9 @@ __device__ __forceinline__ void fft_stage(const float2 *__restrict__ a, float2 *
 }
 
 // Forward FFT of `nlines` lines held in a (stride LS); b is the ping-pong
-// buffer.  Returns the buffer holding the result.
+// buffer.  Returns the buffer holding the result.  RARE enables the radix
+// 7/11/13 stages (only sizes with such factors pay their register cost).
+template <bool RARE>
 __device__ float2 *block_fft(float2 *a, float2 *b, int nlines, int LS, const FFTDesc &f)
 {
     int p = 1;
@@ -169,11 +171,14 @@ __device__ float2 *block_fft(float2 *a, float2 *b, int nlines, int LS, const FFT
         case 3: fft_stage<3>(a, b, nlines, LS, f.n, p, f.tw); break;
         case 4: fft_stage<4>(a, b, nlines, LS, f.n, p, f.tw); break;
         case 5: fft_stage<5>(a, b, nlines, LS, f.n, p, f.tw); break;
-        case 7: fft_stage<7>(a, b, nlines, LS, f.n, p, f.tw); break;
         case 8: fft_stage<8>(a, b, nlines, LS, f.n, p, f.tw); break;
-        case 11: fft_stage<11>(a, b, nlines, LS, f.n, p, f.tw); break;
-        case 13: fft_stage<13>(a, b, nlines, LS, f.n, p, f.tw); break;
-        default: break;
+        default:
+            if (RARE) {
+                if (r == 7) fft_stage<7>(a, b, nlines, LS, f.n, p, f.tw);
+                else if (r == 11) fft_stage<11>(a, b, nlines, LS, f.n, p, f.tw);
+                else if (r == 13) fft_stage<13>(a, b, nlines, LS, f.n, p, f.tw);
+            }
+            break;
         }
         __syncthreads();
         float2 *t = a;
@@ -182,6 +187,13 @@ __device__ float2 *block_fft(float2 *a, float2 *b, int nlines, int LS, const FFT
         p *= r;
     }
     return a;
+}
+
+static bool needs_rare(const FFTDesc &f)
+{
+    for (int s = 0; s < f.nst; ++s)
+        if (f.rad[s] == 7 || f.rad[s] == 11 || f.rad[s] == 13) return true;
+    return false;
 }
 
 __device__ __forceinline__ int slot_of(int n, int N, int K)
@@ -196,6 +208,7 @@ constexpr int kMaxLineCoils = 16;
 
 // FX: image (user layout) * U -> B1, length-K1 FFT along x for one (y,z) line
 // of up to kMaxLineCoils coils.  fNUFT.m:5 + nufft_3d.m:287-289 (j=1).
+template <bool RARE>
 __global__ void __launch_bounds__(kFftThreads)
 k_fx(const float2 *__restrict__ img, const float *__restrict__ U, float2 *__restrict__ B1,
      int N1, int N23, int nc, FFTDesc fd)
@@ -219,7 +232,7 @@ k_fx(const float2 *__restrict__ img, const float *__restrict__ U, float2 *__rest
         A[v * LS + slot_of(n, N1, K)] = make_float2(val.x * w, val.y * w);
     }
     __syncthreads();
-    const float2 *res = block_fft(A, B, nv, LS, fd);
+    const float2 *res = block_fft<RARE>(A, B, nv, LS, fd);
     float2 *ob = B1 + (size_t)line * K * nc + c0;
     for (int t = threadIdx.x; t < K * nv; t += blockDim.x) {
         const int k = t / nv, v = t - k * nv;
@@ -229,6 +242,7 @@ k_fx(const float2 *__restrict__ img, const float *__restrict__ U, float2 *__rest
 
 // IX: B1 -> image, unnormalised inverse FFT along x, crop, *U*scale
 // (+ add_coef * addend).  nufft_3d.m:296-298 (j=1) + aNUFT.m:8-9.
+template <bool RARE>
 __global__ void __launch_bounds__(kFftThreads)
 k_ix(const float2 *__restrict__ B1, const float *__restrict__ U, float2 *__restrict__ img,
      int N1, int N23, int nc, FFTDesc fd, float scale, const float2 *__restrict__ addend,
@@ -247,7 +261,7 @@ k_ix(const float2 *__restrict__ B1, const float *__restrict__ U, float2 *__restr
         A[v * LS + k] = make_float2(val.x, -val.y);
     }
     __syncthreads();
-    const float2 *res = block_fft(A, B, nv, LS, fd);
+    const float2 *res = block_fft<RARE>(A, B, nv, LS, fd);
     const float *Ur = U + (size_t)line * N1;
     for (int t = threadIdx.x; t < N1 * nv; t += blockDim.x) {
         const int v = t / N1, n = t - v * N1;
@@ -265,6 +279,7 @@ k_ix(const float2 *__restrict__ B1, const float *__restrict__ U, float2 *__restr
 }
 
 // Strided pass along y or z over rows of contiguous complex vectors.
+template <bool RARE>
 __global__ void __launch_bounds__(kFftThreads)
 k_line(const float2 *__restrict__ in, float2 *__restrict__ out, LinePass lp, FFTDesc fd, int inv)
 {
@@ -290,7 +305,7 @@ k_line(const float2 *__restrict__ in, float2 *__restrict__ out, LinePass lp, FFT
         A[v * LS + slot] = make_float2(val.x, sg * val.y);
     }
     __syncthreads();
-    const float2 *res = block_fft(A, B, vec, LS, fd);
+    const float2 *res = block_fft<RARE>(A, B, vec, LS, fd);
     for (int t = threadIdx.x; t < lp.n_out * vec; t += blockDim.x) {
         const int o = t / vec, v = t - o * vec;
         const int slot = lp.crop_out ? slot_of(o, lp.Nimg, K) : o;
@@ -346,7 +361,10 @@ static int launch_line(const float2 *in, float2 *out, int n_outer, int64_t rowle
     const int64_t nblk = (int64_t)n_outer * lp.nchunks;
     if (nblk <= 0) return NUFFT3D_SUCCESS;
     if (nblk > 0x7fffffff) return fail(NUFFT3D_ERR_SIZE, "FFT pass grid too large");
-    k_line<<<(unsigned)nblk, kFftThreads, line_smem(lp.vec, fd.n), s>>>(in, out, lp, fd, inv);
+    if (needs_rare(fd))
+        k_line<true><<<(unsigned)nblk, kFftThreads, line_smem(lp.vec, fd.n), s>>>(in, out, lp, fd, inv);
+    else
+        k_line<false><<<(unsigned)nblk, kFftThreads, line_smem(lp.vec, fd.n), s>>>(in, out, lp, fd, inv);
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }
@@ -357,7 +375,10 @@ int launch_fx(nufft3d_plan *p, const float2 *img, float2 *B1, int nc, cudaStream
     const FFTDesc &fd = p->fft[0];
     const int nv = nc < kMaxLineCoils ? nc : kMaxLineCoils;
     dim3 grid(N23, (nc + kMaxLineCoils - 1) / kMaxLineCoils);
-    k_fx<<<grid, kFftThreads, line_smem(nv, fd.n), s>>>(img, p->U, B1, N1, N23, nc, fd);
+    if (needs_rare(fd))
+        k_fx<true><<<grid, kFftThreads, line_smem(nv, fd.n), s>>>(img, p->U, B1, N1, N23, nc, fd);
+    else
+        k_fx<false><<<grid, kFftThreads, line_smem(nv, fd.n), s>>>(img, p->U, B1, N1, N23, nc, fd);
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }
@@ -369,8 +390,12 @@ int launch_ix(nufft3d_plan *p, const float2 *B1, float2 *img, int nc, float scal
     const FFTDesc &fd = p->fft[0];
     const int nv = nc < kMaxLineCoils ? nc : kMaxLineCoils;
     dim3 grid(N23, (nc + kMaxLineCoils - 1) / kMaxLineCoils);
-    k_ix<<<grid, kFftThreads, line_smem(nv, fd.n), s>>>(B1, p->U, img, N1, N23, nc, fd, scale,
-                                                        addend, add_coef);
+    if (needs_rare(fd))
+        k_ix<true><<<grid, kFftThreads, line_smem(nv, fd.n), s>>>(B1, p->U, img, N1, N23, nc, fd, scale,
+                                                                addend, add_coef);
+    else
+        k_ix<false><<<grid, kFftThreads, line_smem(nv, fd.n), s>>>(B1, p->U, img, N1, N23, nc, fd, scale,
+                                                                 addend, add_coef);
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }
@@ -414,9 +439,12 @@ int launch_iy(nufft3d_plan *p, const float2 *B2, float2 *B1, int nc, cudaStream_
 int configure_fft_kernels()
 {
     const int max_smem = 227 * 1024;
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fx, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_ix, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fx<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_ix<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fx<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_ix<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
     return NUFFT3D_SUCCESS;
 }
 

@@ -241,6 +241,7 @@ int run_inverse(nufft3d_plan *p, const float2 *raw, float2 *x, int nc, int maxit
 
 size_t smem_interp_bytes(const Geom &g, int cb);
 size_t cand_smem_bytes(int n);
+size_t smem_plane_bytes(int R, int cb);
 
 // Stage timing scope: records an event pair on stream s when profiling is on
 // (and the stream is not being captured into a graph).

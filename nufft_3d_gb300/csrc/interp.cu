@@ -25,6 +25,16 @@ namespace nufft3d {
 constexpr int kInterpThreads = 1024;
 constexpr int kGroup = 8;                 // lanes sharing one sample
 
+// Tile plane stride (points per coil plane) as a compile-time constant per
+// half-width R: tiles are 8^3 (3-D) or 32x32x1 (2-D) plus the halo, and the
+// stride covers both, so each coil plane is an immediate offset.
+template <int R>
+struct Plane {
+    static constexpr int P3 = (8 + 2 * R) * (8 + 2 * R) * (8 + 2 * R);
+    static constexpr int P2 = (32 + 2 * R) * (32 + 2 * R);
+    static constexpr int PS = P3 > P2 ? P3 : P2;
+};
+
 __device__ __forceinline__ int wrap_idx(int x, int K)
 {
     x %= K;
@@ -137,15 +147,15 @@ __device__ __forceinline__ void for_tile_rows(const Geom &g, int ox, int oy, int
 
 // Gather: tile staged coil-major ([CB][P^3] complex) -> ks.  kGroup lanes per
 // sample walk the candidate list; partial sums are reduced across the group.
-template <int CB, bool RADIAL>
+template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
 k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
          const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
          KBParams kb, float scale, const float *__restrict__ wsample, Cand cd)
 {
     extern __shared__ float4 smem4[];
+    constexpr int pv = Plane<R>::PS;
     const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
-    const int pv = PxPy * g.P[2];
     CandSmem cs;
     cs.f = smem4;
     cs.off = reinterpret_cast<int *>(smem4 + cd.n);
@@ -157,10 +167,19 @@ k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
     const int tz = tid / (g.nt[0] * g.nt[1]);
     const int ox = tx * g.T[0] - g.Ra[0], oy = ty * g.T[1] - g.Ra[1], oz = tz * g.T[2] - g.Ra[2];
     const int cb = min(CB, nc - c0);
-    build_cand(cd, cs, Px, PxPy);
+    // stage the padded tile with asynchronous copies (no register round trip)
     for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int c, size_t gidx) {
-        tile[c * pv + pt] = c < cb ? G[gidx * nc + c0 + c] : make_float2(0.f, 0.f);
+        float2 *dst = &tile[c * pv + pt];
+        if (c < cb) {
+            const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(&G[gidx * nc + c0 + c]) : "memory");
+        } else {
+            *dst = make_float2(0.f, 0.f);
+        }
     });
+    asm volatile("cp.async.commit_group;" ::: "memory");
+    build_cand(cd, cs, Px, PxPy);
+    asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int lig = lane & (kGroup - 1);
@@ -253,7 +272,7 @@ __device__ __forceinline__ int to_fixed(float v)
     return __float_as_int(v + 12582912.0f) - 0x4B400000;
 }
 
-template <int CB, bool RADIAL>
+template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
 k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
          const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
@@ -261,8 +280,8 @@ k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
 {
     extern __shared__ float4 smem4[];
     __shared__ float red[33];
+    constexpr int pv = Plane<R>::PS;
     const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
-    const int pv = PxPy * g.P[2];
     CandSmem cs;
     cs.f = smem4;
     cs.off = reinterpret_cast<int *>(smem4 + cd.n);
@@ -444,35 +463,63 @@ size_t smem_interp_bytes(const Geom &g, int cb)
 
 static Cand cand_of(const nufft3d_plan *p) { return Cand{p->cand, p->n_cand}; }
 
-template <int CB, bool RADIAL>
+size_t smem_plane_bytes(int R, int cb)
+{
+    int ps = 0;
+    switch (R) {
+    case 1: ps = Plane<1>::PS; break;
+    case 2: ps = Plane<2>::PS; break;
+    case 3: ps = Plane<3>::PS; break;
+    default: ps = Plane<4>::PS; break;
+    }
+    return (size_t)ps * cb * sizeof(float2);
+}
+
+template <int CB, bool RADIAL, int R>
 static int gather_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, int c0, float scale,
                     const float *ws, cudaStream_t s)
 {
-    const size_t smem = smem_interp_bytes(p->geom, CB) + cand_smem_bytes(p->n_cand);
-    k_gather<CB, RADIAL><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
+    const size_t smem = smem_plane_bytes(R, CB) + cand_smem_bytes(p->n_cand);
+    k_gather<CB, RADIAL, R><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
         G, ks, nc, c0, p->samples, p->blocks, p->geom, p->kb, scale, ws, cand_of(p));
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }
 
-template <int CB, bool RADIAL>
+template <int CB, bool RADIAL, int R>
 static int spread_t(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, int c0, cudaStream_t s)
 {
-    const size_t smem = smem_interp_bytes(p->geom, CB) + cand_smem_bytes(p->n_cand);
-    k_spread<CB, RADIAL><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
+    const size_t smem = smem_plane_bytes(R, CB) + cand_smem_bytes(p->n_cand);
+    k_spread<CB, RADIAL, R><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
         ks, G, nc, c0, p->samples, p->blocks, p->geom, p->kb, cand_of(p));
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
+}
+
+template <bool GATHER, int CB, bool RADIAL>
+static int dispatch_r(nufft3d_plan *p, const float2 *in, float2 *out, int nc, int c0, float scale,
+                      const float *ws, cudaStream_t s)
+{
+    switch (p->geom.R) {
+    case 1: return GATHER ? gather_t<CB, RADIAL, 1>(p, in, out, nc, c0, scale, ws, s)
+                          : spread_t<CB, RADIAL, 1>(p, in, out, nc, c0, s);
+    case 2: return GATHER ? gather_t<CB, RADIAL, 2>(p, in, out, nc, c0, scale, ws, s)
+                          : spread_t<CB, RADIAL, 2>(p, in, out, nc, c0, s);
+    case 3: return GATHER ? gather_t<CB, RADIAL, 3>(p, in, out, nc, c0, scale, ws, s)
+                          : spread_t<CB, RADIAL, 3>(p, in, out, nc, c0, s);
+    default:
+        if (CB == 8) return fail(NUFFT3D_ERR_UNSUPPORTED, "8 coils per pass do not fit with R=4 tiles");
+        return GATHER ? gather_t<(CB < 8 ? CB : 4), RADIAL, 4>(p, in, out, nc, c0, scale, ws, s)
+                      : spread_t<(CB < 8 ? CB : 4), RADIAL, 4>(p, in, out, nc, c0, s);
+    }
 }
 
 template <bool GATHER, int CB>
 static int dispatch(nufft3d_plan *p, const float2 *in, float2 *out, int nc, int c0, float scale,
                     const float *ws, cudaStream_t s)
 {
-    const bool rad = p->geom.radial != 0;
-    if (GATHER) return rad ? gather_t<CB, true>(p, in, out, nc, c0, scale, ws, s)
-                           : gather_t<CB, false>(p, in, out, nc, c0, scale, ws, s);
-    return rad ? spread_t<CB, true>(p, in, out, nc, c0, s) : spread_t<CB, false>(p, in, out, nc, c0, s);
+    return p->geom.radial ? dispatch_r<GATHER, CB, true>(p, in, out, nc, c0, scale, ws, s)
+                          : dispatch_r<GATHER, CB, false>(p, in, out, nc, c0, scale, ws, s);
 }
 
 template <bool GATHER>
@@ -545,14 +592,30 @@ int launch_permute_in(nufft3d_plan *p, const float2 *k, float2 *ks, int nc,
     return NUFFT3D_SUCCESS;
 }
 
+template <int CB, bool RADIAL, int R>
+static int cfg_one()
+{
+    const int mx = 227 * 1024 - 2048; // leave room for static shared memory
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_gather<CB, RADIAL, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_spread<CB, RADIAL, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    return NUFFT3D_SUCCESS;
+}
+
+template <int CB, bool RADIAL>
+static int cfg_r()
+{
+    NUFFT_TRY((cfg_one<CB, RADIAL, 1>()));
+    NUFFT_TRY((cfg_one<CB, RADIAL, 2>()));
+    NUFFT_TRY((cfg_one<CB, RADIAL, 3>()));
+    NUFFT_TRY((cfg_one<(CB < 8 ? CB : 4), RADIAL, 4>()));
+    return NUFFT3D_SUCCESS;
+}
+
 template <int CB>
 static int cfg_cb()
 {
-    const int mx = 227 * 1024 - 2048; // leave room for static shared memory
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_gather<CB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_gather<CB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_spread<CB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_spread<CB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    NUFFT_TRY((cfg_r<CB, true>()));
+    NUFFT_TRY((cfg_r<CB, false>()));
     return NUFFT3D_SUCCESS;
 }
 

@@ -639,9 +639,11 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
     for (int a = 0; a < 3; ++a) {
         g.K[a] = K[a];
         g.Ra[a] = (a == 2 && is2d) ? 0 : R;
-        int t = o.tile[a] > 0 ? o.tile[a] : (is2d ? (a == 2 ? 1 : 32) : 8);
-        if (a == 2 && is2d) t = 1;
-        if (t > 64) t = 64;
+        const int t = is2d ? (a == 2 ? 1 : 32) : 8; // the kernels' fixed tile shape
+        if (o.tile[a] > 0 && o.tile[a] != t) {
+            delete p;
+            return fail(NUFFT3D_ERR_UNSUPPORTED, "tile shape is fixed at 8x8x8 (3-D) / 32x32x1 (2-D)");
+        }
         g.T[a] = t;
         g.P[a] = t + 2 * g.Ra[a];
         g.nt[a] = (K[a] + t - 1) / t;
@@ -659,8 +661,8 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
     while (cb * 2 <= cpp && cb < 8) cb *= 2;
     // the kernels also hold the candidate tables (<= 461 taps for R <= 4)
     const size_t cand_max = cand_smem_bytes(R <= 2 ? 128 : (R == 3 ? 256 : 512));
-    while (cb > 1 && smem_interp_bytes(g, cb) + cand_max > 210 * 1024) cb /= 2;
-    if (smem_interp_bytes(g, cb) + cand_max > 227 * 1024) {
+    while (cb > 1 && smem_plane_bytes(R, cb) + cand_max > 210 * 1024) cb /= 2;
+    if (smem_plane_bytes(R, cb) + cand_max > 220 * 1024) {
         delete p;
         return fail(NUFFT3D_ERR_UNSUPPORTED, "interpolation tile too large for shared memory");
     }
