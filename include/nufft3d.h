@@ -28,6 +28,7 @@
 #ifndef NUFFT3D_H
 #define NUFFT3D_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -112,6 +113,25 @@ int nufft3d_adjoint(nufft3d_plan *plan, const float *k_dev, float *x_dev, int nc
  * y = aNUFT(W.*fNUFT(x)) + damp^2*x.  W_dev: [M] or NULL for W = d. */
 int nufft3d_normal(nufft3d_plan *plan, const float *x_dev, float *y_dev, int nc,
                    double damp, const float *W_dev, void *stream);
+
+/* k = obj.fNUFT(x) without any device allocation in the call.  No counterpart
+ * in the reference (MATLAB allocates freely); it exists for callers that must
+ * not trigger cudaMalloc -- it synchronises the whole device and can fail under
+ * memory pressure -- such as a latency-critical reconstruction loop or a host
+ * application that owns all GPU memory through its own pool.  Same arguments
+ * and result as nufft3d_forward.  Work buffers come from one fixed array in
+ * the library's device image, nufft3d_forward_noalloc_scratch_bytes() bytes
+ * per GPU (held by every GPU that loads the library until exit); plans/coil
+ * counts that need more return NUFFT3D_ERR_SIZE.  Every call on a device
+ * shares that array: calls that overlap on the GPU race and must be
+ * serialised by the caller.  The first call on each device looks up the
+ * array's address (cudaGetSymbolAddress); make it before any stream capture.
+ * The plan itself is created beforehand with nufft3d_plan_create. */
+int nufft3d_forward_noalloc(nufft3d_plan *plan, const float *x_dev, float *k_dev, int nc,
+                            void *stream);
+
+/* Size in bytes of the fixed scratch array used by nufft3d_forward_noalloc. */
+size_t nufft3d_forward_noalloc_scratch_bytes(void);
 
 /* Host-pointer variants of fNUFT / aNUFT: copy in, run, copy out, synchronise. */
 int nufft3d_forward_host(nufft3d_plan *plan, const float *x_host, float *k_host, int nc);

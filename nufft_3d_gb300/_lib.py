@@ -63,6 +63,8 @@ SIGNATURES = {
     "nufft3d_forward": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, _P]),
     "nufft3d_adjoint": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, _P]),
     "nufft3d_normal": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_double, _P, _P]),
+    "nufft3d_forward_noalloc": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, _P]),
+    "nufft3d_forward_noalloc_scratch_bytes": (ctypes.c_size_t, []),
     "nufft3d_forward_host": (ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
     "nufft3d_adjoint_host": (ctypes.c_int, [_P, _P, _P, ctypes.c_int]),
     "nufft3d_inverse": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_double, _P,
