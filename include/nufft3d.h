@@ -93,6 +93,18 @@ int nufft3d_plan_create(const double *om_host, int64_t M, const int32_t *N, int 
 
 int nufft3d_plan_destroy(nufft3d_plan *plan);
 
+/* A second handle on the same trajectory: shares the source plan's device
+ * tables (sorted samples, tiles, U, d, twiddles; freed with the last handle)
+ * and has its own work buffers and stream, so calls on the two handles may
+ * run concurrently.  Used by the serving loop for concurrent reconstructions
+ * of one resident trajectory.  nufft3d_density on any handle changes the
+ * shared d. */
+int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **plan);
+
+/* Device bytes a handle allocates for work buffers at nc coils (FFT and
+ * interpolation scratch; plus the iNUFT solver vectors if with_solver). */
+int nufft3d_plan_footprint(const nufft3d_plan *plan, int nc, int with_solver, int64_t *bytes);
+
 int nufft3d_plan_info(const nufft3d_plan *plan, nufft3d_info *info);
 
 /* obj.U (deap.m:2-36,98): [N1 N2 N3] real single, copied to host. */

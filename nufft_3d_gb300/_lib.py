@@ -57,6 +57,8 @@ SIGNATURES = {
     "nufft3d_plan_create": (ctypes.c_int, [_P, ctypes.c_int64, _P, ctypes.c_int, ctypes.POINTER(Opts),
                                            ctypes.POINTER(ctypes.c_void_p)]),
     "nufft3d_plan_destroy": (ctypes.c_int, [_P]),
+    "nufft3d_plan_share": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_void_p)]),
+    "nufft3d_plan_footprint": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
     "nufft3d_plan_info": (ctypes.c_int, [_P, ctypes.POINTER(Info)]),
     "nufft3d_get_deap": (ctypes.c_int, [_P, _P]),
     "nufft3d_get_density": (ctypes.c_int, [_P, _P]),

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -160,6 +161,15 @@ struct SolverWork {
     int nchunk = 0;
 };
 
+// Device tables of a plan that never change after creation (sorted samples,
+// tile pieces, candidate taps, U, d, twiddles).  Plans made with
+// nufft3d_plan_share hold the same TableOwner; the last one frees them.
+struct TableOwner {
+    int device = 0;
+    std::vector<void *> ptrs;
+    ~TableOwner();
+};
+
 } // namespace nufft3d
 
 struct nufft3d_plan {
@@ -193,6 +203,7 @@ struct nufft3d_plan {
     int64_t table_bytes = 0;
     cudaStream_t own_stream = nullptr;
     nufft3d::Profiler prof;
+    std::shared_ptr<nufft3d::TableOwner> tables;  // owner of the pointers above marked as tables
 };
 
 namespace nufft3d {

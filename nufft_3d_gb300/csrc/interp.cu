@@ -145,6 +145,43 @@ __device__ __forceinline__ void for_tile_rows(const Geom &g, int ox, int oy, int
     }
 }
 
+// Work layout shared by gather and spread: one warp per sample.  All 32
+// lanes evaluate 32 candidate taps at a time (weight + tile offset); the hits
+// are compacted through a per-warp queue and then applied by sub-steps in
+// which lane (q, j) handles queued tap j for coil pair q (NP pairs, CPS taps
+// per sub-step).  Quarter-warps therefore touch 8 neighbouring tile points of
+// one coil plane, which keeps shared-memory accesses free of bank conflicts.
+template <int CB>
+struct Lanes {
+    static constexpr int NP = CB >= 2 ? CB / 2 : 1;  // coil pairs (or one coil)
+    static constexpr int CPS = 32 / NP;               // queued taps per sub-step
+};
+
+struct TapQueue {
+    float w[32];
+    int off[32];
+};
+
+// Evaluate candidates [base, base+32) of sample sg; returns the number of hits
+// written to the warp's queue (in lane order).
+template <bool RADIAL>
+__device__ __forceinline__ int eval_chunk(int base, const SampleGeo &sg, const CandSmem &cs, int ncand,
+                                          const KBParams &kb, TapQueue &qu, int lane)
+{
+    const int ci = base + lane;
+    float w = 0.f;
+    int off = 0;
+    const bool hit = ci < ncand && tap<RADIAL>(ci, sg, cs, kb, w, off);
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (hit) {
+        const int r = __popc(m & ((1u << lane) - 1u));
+        qu.w[r] = w;
+        qu.off[r] = off;
+    }
+    __syncwarp();
+    return __popc(m);
+}
+
 // Gather: tile staged coil-major ([CB][P^3] complex) -> ks.  kGroup lanes per
 // sample walk the candidate list; partial sums are reduced across the group.
 template <int CB, bool RADIAL, int R>
@@ -272,20 +309,30 @@ __device__ __forceinline__ int to_fixed(float v)
     return __float_as_int(v + 12582912.0f) - 0x4B400000;
 }
 
+// Integer planes of the spread: one plane per (coil, re/im); the stride is
+// the smallest value >= the tile volume that is 2 mod 32, so a warp's 32
+// reductions (8 neighbouring points x 4 planes 2 apart) hit 32 distinct banks.
+template <int R>
+struct IPlane {
+    static constexpr int PS = ((Plane<R>::PS + 29) / 32) * 32 + 2;
+};
+
 template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
 k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
          const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
          KBParams kb, Cand cd)
 {
+    constexpr int NP = Lanes<CB>::NP, CPS = Lanes<CB>::CPS;
+    constexpr int ps = IPlane<R>::PS;
     extern __shared__ float4 smem4[];
     __shared__ float red[33];
-    constexpr int pv = Plane<R>::PS;
+    __shared__ TapQueue queues[kInterpThreads / 32];
     const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
     CandSmem cs;
     cs.f = smem4;
     cs.off = reinterpret_cast<int *>(smem4 + cd.n);
-    int *tile = cs.off + 8 * cd.n;
+    int *tile = reinterpret_cast<int *>(smem4 + cd.n + 2 * cd.n);
     const int4 bi = blocks[blockIdx.x];
     const int tid = bi.x;
     const int tx = tid % g.nt[0];
@@ -302,7 +349,7 @@ k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
             m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
         }
     }
-    for (int t = threadIdx.x; t < pv * CB * 2; t += blockDim.x) tile[t] = 0;
+    for (int t = threadIdx.x; t < ps * CB * 2; t += blockDim.x) tile[t] = 0;
     build_cand(cd, cs, Px, PxPy);
     const float ymax = block_max(m, red);   // contains __syncthreads
     if (!(ymax > 0.f)) return;             // nothing to add (block-uniform)
@@ -312,72 +359,62 @@ k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
     frexpf(ymax * wsum, &ecy);             // wsum*ymax < 2^ecy
     const int F = min(22 - ey, 30 - ecy);
     const float scale = ldexpf(1.f, F), inv_scale = ldexpf(1.f, -F);
-    const int lane = threadIdx.x & 31;
-    const int lig = lane & (kGroup - 1);
-    const int grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
-    const int niter = (cd.n + kGroup - 1) / kGroup;
-    const int rot = ((lane / kGroup) * niter) / (32 / kGroup);
-    float4 rec_next = make_float4(0.f, 0.f, 0.f, 0.f);
-    float2 y_next[CB];
-    auto fetch = [&](int s) {
-        rec_next = __ldg(&samples[s]);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const int q = lane / CPS, j = lane % CPS;
+    const int c = CB >= 2 ? 2 * q : 0;
+    int *pl0 = tile + (size_t)(2 * c) * ps;  // re, im of coil c; then re, im of coil c+1
+    TapQueue &qu = queues[warp];
+    auto load_y = [&](int s, float4 &y) {
         const float2 *src = ks + (size_t)s * nc + c0;
-#pragma unroll
-        for (int c = 0; c < CB; ++c) {
-            const float2 v = c < cb ? src[c] : make_float2(0.f, 0.f);
-            y_next[c] = make_float2(v.x * scale, v.y * scale);
-        }
+        const float2 a = c < cb ? src[c] : make_float2(0.f, 0.f);
+        const float2 b = (CB >= 2 && c + 1 < cb) ? src[c + 1] : make_float2(0.f, 0.f);
+        y = make_float4(a.x * scale, a.y * scale, b.x * scale, b.y * scale);
     };
-    if (bi.y + grp < send) fetch(bi.y + grp);
-    for (int s = bi.y + grp; s < send; s += ngrp) {
+    float4 rec_next = make_float4(0.f, 0.f, 0.f, 0.f), y_next = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (bi.y + warp < send) {
+        rec_next = __ldg(&samples[bi.y + warp]);
+        load_y(bi.y + warp, y_next);
+    }
+    for (int s = bi.y + warp; s < send; s += nwarps) {
         const SampleGeo sg = sample_geo(rec_next, Px, g.P[1]);
-        float2 yv[CB];
-#pragma unroll
-        for (int c = 0; c < CB; ++c) yv[c] = y_next[c];
-        if (s + ngrp < send) fetch(s + ngrp);
-        for (int it0 = 0; it0 < niter; it0 += 2) {
-            int ita = it0 + rot, itb = it0 + 1 + rot;
-            if (ita >= niter) ita -= niter;
-            if (itb >= niter) itb -= niter;
-            const int ci0 = ita * kGroup + lig, ci1 = itb * kGroup + lig;
-            float w0, w1;
-            int off0, off1;
-            const bool h0 = ci0 < cd.n && tap<RADIAL>(ci0, sg, cs, kb, w0, off0);
-            const bool h1 = it0 + 1 < niter && ci1 < cd.n && tap<RADIAL>(ci1, sg, cs, kb, w1, off1);
-            if (h0) {
-#pragma unroll
-                for (int c = 0; c < CB; ++c) {
-                    red_add(&tile[(2 * c) * pv + off0], to_fixed(w0 * yv[c].x));
-                    red_add(&tile[(2 * c + 1) * pv + off0], to_fixed(w0 * yv[c].y));
+        const float4 y = y_next;
+        if (s + nwarps < send) {
+            rec_next = __ldg(&samples[s + nwarps]);
+            load_y(s + nwarps, y_next);
+        }
+        for (int base = 0; base < cd.n; base += 32) {
+            const int nh = eval_chunk<RADIAL>(base, sg, cs, cd.n, kb, qu, lane);
+            for (int t = j; t < nh; t += CPS) {
+                const float w = qu.w[t];
+                const int off = qu.off[t];
+                red_add(pl0 + off, to_fixed(w * y.x));
+                red_add(pl0 + ps + off, to_fixed(w * y.y));
+                if (CB >= 2) {
+                    red_add(pl0 + 2 * ps + off, to_fixed(w * y.z));
+                    red_add(pl0 + 3 * ps + off, to_fixed(w * y.w));
                 }
             }
-            if (h1) {
-#pragma unroll
-                for (int c = 0; c < CB; ++c) {
-                    red_add(&tile[(2 * c) * pv + off1], to_fixed(w1 * yv[c].x));
-                    red_add(&tile[(2 * c + 1) * pv + off1], to_fixed(w1 * yv[c].y));
-                }
-            }
+            __syncwarp();
         }
     }
     __syncthreads();
     const int ox = tx * g.T[0] - g.Ra[0], oy = ty * g.T[1] - g.Ra[1], oz = tz * g.T[2] - g.Ra[2];
     if (CB % 2 == 0 && nc % 2 == 0 && c0 % 2 == 0) {
         for_tile_rows<CB / 2>(g, ox, oy, oz, [&](int pt, int cq, size_t gidx) {
-            const int c = 2 * cq;
-            if (c >= cb) return;
-            const int a = tile[(2 * c) * pv + pt], b = tile[(2 * c + 1) * pv + pt];
-            const int e = tile[(2 * c + 2) * pv + pt], f = tile[(2 * c + 3) * pv + pt];
+            const int cc = 2 * cq;
+            if (cc >= cb) return;
+            const int a = tile[(2 * cc) * ps + pt], b = tile[(2 * cc + 1) * ps + pt];
+            const int e = tile[(2 * cc + 2) * ps + pt], f = tile[(2 * cc + 3) * ps + pt];
             if ((a | b | e | f) == 0) return;
-            atomicAdd(reinterpret_cast<float4 *>(&G[gidx * nc + c0 + c]),
+            atomicAdd(reinterpret_cast<float4 *>(&G[gidx * nc + c0 + cc]),
                       make_float4(a * inv_scale, b * inv_scale, e * inv_scale, f * inv_scale));
         });
     } else {
-        for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int c, size_t gidx) {
-            if (c >= cb) return;
-            const int a = tile[(2 * c) * pv + pt], b = tile[(2 * c + 1) * pv + pt];
+        for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int cc, size_t gidx) {
+            if (cc >= cb) return;
+            const int a = tile[(2 * cc) * ps + pt], b = tile[(2 * cc + 1) * ps + pt];
             if ((a | b) == 0) return;
-            atomicAdd(&G[gidx * nc + c0 + c], make_float2(a * inv_scale, b * inv_scale));
+            atomicAdd(&G[gidx * nc + c0 + cc], make_float2(a * inv_scale, b * inv_scale));
         });
     }
 }
@@ -396,7 +433,7 @@ k_weight_sum(const float4 *__restrict__ samples, int4 *__restrict__ blocks, Geom
     CandSmem cs;
     cs.f = smem4;
     cs.off = reinterpret_cast<int *>(smem4 + cd.n);
-    float *tile = reinterpret_cast<float *>(cs.off + 8 * cd.n);
+    float *tile = reinterpret_cast<float *>(smem4 + cd.n + 2 * cd.n);
     const int4 bi = blocks[blockIdx.x];
     for (int t = threadIdx.x; t < pv; t += blockDim.x) tile[t] = 0.f;
     build_cand(cd, cs, Px, PxPy);
@@ -489,7 +526,7 @@ static int gather_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, int c0
 template <int CB, bool RADIAL, int R>
 static int spread_t(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, int c0, cudaStream_t s)
 {
-    const size_t smem = smem_plane_bytes(R, CB) + cand_smem_bytes(p->n_cand);
+    const size_t smem = (size_t)IPlane<R>::PS * CB * 2 * sizeof(int) + cand_smem_bytes(p->n_cand);
     k_spread<CB, RADIAL, R><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
         ks, G, nc, c0, p->samples, p->blocks, p->geom, p->kb, cand_of(p));
     NUFFT_CUDA_TRY(cudaGetLastError());
@@ -592,12 +629,22 @@ int launch_permute_in(nufft3d_plan *p, const float2 *k, float2 *ks, int nc,
     return NUFFT3D_SUCCESS;
 }
 
+// Allow each kernel all the shared memory a block can have, less its static part.
+template <typename K>
+static int allow_smem(K kernel)
+{
+    cudaFuncAttributes fa;
+    NUFFT_CUDA_TRY(cudaFuncGetAttributes(&fa, kernel));
+    const int mx = 227 * 1024 - (int)fa.sharedSizeBytes;
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    return NUFFT3D_SUCCESS;
+}
+
 template <int CB, bool RADIAL, int R>
 static int cfg_one()
 {
-    const int mx = 227 * 1024 - 2048; // leave room for static shared memory
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_gather<CB, RADIAL, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_spread<CB, RADIAL, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    NUFFT_TRY(allow_smem(k_gather<CB, RADIAL, R>));
+    NUFFT_TRY(allow_smem(k_spread<CB, RADIAL, R>));
     return NUFFT3D_SUCCESS;
 }
 
@@ -621,8 +668,8 @@ static int cfg_cb()
 
 int configure_interp_kernels()
 {
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_weight_sum<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - 2048));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_weight_sum<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024 - 2048));
+    NUFFT_TRY(allow_smem(k_weight_sum<true>));
+    NUFFT_TRY(allow_smem(k_weight_sum<false>));
     NUFFT_TRY(cfg_cb<1>());
     NUFFT_TRY(cfg_cb<2>());
     NUFFT_TRY(cfg_cb<4>());

@@ -99,11 +99,15 @@ static std::vector<double> deap_host(const int N[3], const int K[3], double J, d
                         kernel_host(dz2, alpha, J);
                 T[((size_t)dz * nJ + dy) * nJ + dx] = v;
             }
-    auto coef = [&](int axis, int d, int p) {
-        if (d == 0) return 0.5;
-        const double m = p - N[axis] / 2;
-        return std::cos(M_PI * d * m / K[axis]);
-    };
+    // per-axis coefficient tables c_a(d, p) = 0.5 (d = 0) or cos(pi d (p - N/2) / K)
+    std::vector<double> ctab[3];
+    for (int a = 0; a < 3; ++a) {
+        ctab[a].resize((size_t)nJ * std::max(N[a], 1));
+        for (int d = 0; d < nJ; ++d)
+            for (int p = 0; p < N[a]; ++p)
+                ctab[a][(size_t)d * N[a] + p] = d == 0 ? 0.5 : std::cos(M_PI * d * (double)(p - N[a] / 2) / K[a]);
+    }
+    auto coef = [&](int axis, int d, int p) { return ctab[axis][(size_t)d * N[axis] + p]; };
     const int N1 = N[0], N2 = N[1], N3 = N[2];
     // x
     std::vector<double> A((size_t)N1 * nJ * nz, 0.0);
@@ -314,21 +318,44 @@ int configure_kernels()
     return NUFFT3D_SUCCESS;
 }
 
+TableOwner::~TableOwner()
+{
+    int prev = -1;
+    if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+    if (prev != device) cudaSetDevice(device);
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    if (prev >= 0 && prev != device) cudaSetDevice(prev);
+}
+
+// Hand the plan's table pointers to a shared owner (after a successful build).
+static void adopt_tables(nufft3d_plan *p)
+{
+    auto t = std::make_shared<TableOwner>();
+    t->device = p->device;
+    t->ptrs = {p->samples, p->perm, p->inv, p->blocks, p->cand, p->U, p->d, p->d_orig,
+               p->tw[0], p->tw[1], p->tw[2]};
+    p->tables = t;
+}
+
+// Free what the plan owns by itself; tables go with the last sharer.
 static void free_plan_memory(nufft3d_plan *p)
 {
     auto F = [](void *ptr) {
         if (ptr) cudaFree(ptr);
     };
-    F(p->samples);
-    F(p->perm);
-    F(p->inv);
-    F(p->blocks);
-    F(p->cand);
-    F(p->U);
-    F(p->d);
-    F(p->d_orig);
+    if (!p->tables) { // never adopted: free tables directly
+        F(p->samples);
+        F(p->perm);
+        F(p->inv);
+        F(p->blocks);
+        F(p->cand);
+        F(p->U);
+        F(p->d);
+        F(p->d_orig);
+        for (int a = 0; a < 3; ++a) F(p->tw[a]);
+    }
     F(p->wbuf);
-    for (int a = 0; a < 3; ++a) F(p->tw[a]);
     F(p->scratch.B1);
     F(p->scratch.B2);
     if (p->scratch.G != p->scratch.B2) F(p->scratch.G); // 2D: G aliases B2
@@ -340,6 +367,7 @@ static void free_plan_memory(nufft3d_plan *p)
     F(w.partial); F(w.scal); F(w.iters);
     profile_release(p);
     if (p->own_stream) cudaStreamDestroy(p->own_stream);
+    p->tables.reset();
 }
 
 struct DeviceGuard {
@@ -678,6 +706,7 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
         delete p;
         return fail(st, msg);
     }
+    adopt_tables(p);
     if (o.verbose) {
         std::printf(" Created nufft_3d plan: N=[%d %d %d] K=[%d %d %d] J=%g u=%g alpha=%g radial=%d\n",
                     N[0], N[1], N[2], K[0], K[1], K[2], o.J, o.u, alpha, p->radial);
@@ -685,6 +714,65 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
                     (long long)p->nnz, (long long)M, p->taps, (long long)p->n_blocks);
     }
     *out = p;
+    return NUFFT3D_SUCCESS;
+}
+
+extern "C" int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **out)
+{
+    clear_error();
+    if (!src || !out) return fail(NUFFT3D_ERR_ARG, "NULL argument");
+    *out = nullptr;
+    DeviceGuard guard(src->device);
+    nufft3d_plan *p = new nufft3d_plan();
+    p->device = src->device;
+    for (int a = 0; a < 3; ++a) p->N[a] = src->N[a];
+    p->M = src->M;
+    p->nnz = src->nnz;
+    p->J = src->J;
+    p->u = src->u;
+    p->alpha = src->alpha;
+    p->i0a = src->i0a;
+    p->radial = src->radial;
+    p->geom = src->geom;
+    p->kb = src->kb;
+    p->samples = src->samples;
+    p->perm = src->perm;
+    p->inv = src->inv;
+    p->blocks = src->blocks;
+    p->n_blocks = src->n_blocks;
+    p->cand = src->cand;
+    p->n_cand = src->n_cand;
+    p->coils_per_pass = src->coils_per_pass;
+    p->taps = src->taps;
+    p->U = src->U;
+    p->d = src->d;
+    p->d_orig = src->d_orig;
+    for (int a = 0; a < 3; ++a) {
+        p->tw[a] = src->tw[a];
+        p->fft[a] = src->fft[a];
+    }
+    p->table_bytes = src->table_bytes;
+    p->tables = src->tables;
+    if (cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        p->tables.reset();
+        delete p;
+        return fail(NUFFT3D_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    *out = p;
+    return NUFFT3D_SUCCESS;
+}
+
+extern "C" int nufft3d_plan_footprint(const nufft3d_plan *p, int nc, int with_solver, int64_t *bytes)
+{
+    clear_error();
+    if (!p || !bytes || nc < 1) return fail(NUFFT3D_ERR_ARG, "invalid argument");
+    const int64_t K1 = p->geom.K[0], K2 = p->geom.K[1], K3 = p->geom.K[2];
+    const int64_t N1 = p->N[0], N2 = p->N[1], N3 = p->N[2];
+    const int64_t c8 = 8 * (int64_t)nc;
+    int64_t b = (K1 * N2 * N3 + K1 * K2 * N3 + (p->geom.is2d ? 0 : K1 * K2 * K3)) * c8 +
+                (p->nnz > 0 ? p->nnz : 1) * c8;
+    if (with_solver) b += 7 * N1 * N2 * N3 * c8 + 4 * p->nnz;
+    *bytes = b;
     return NUFFT3D_SUCCESS;
 }
 

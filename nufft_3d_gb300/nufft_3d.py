@@ -124,7 +124,8 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
     # --------------------------------------------------------- lifecycle
     def close(self):
         if getattr(self, "_plan", None):
-            self._L.nufft3d_plan_destroy(self._plan)
+            if not getattr(self, "_borrowed", False):
+                self._L.nufft3d_plan_destroy(self._plan)
             self._plan = None
 
     def __del__(self):
@@ -132,6 +133,22 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
             self.close()
         except Exception:
             pass
+
+    def share(self):
+        """A second object on the same resident trajectory tables with its own
+        work buffers and stream (nufft3d_plan_share); safe to use concurrently."""
+        h = ctypes.c_void_p()
+        _lib.check(self._L.nufft3d_plan_share(self.plan, ctypes.byref(h)))
+        t = object.__new__(nufft_3d)
+        t.__dict__.update(self.__dict__)
+        t._plan = h
+        t._adjoint = False
+        return t
+
+    def footprint(self, nc, with_solver=True):
+        b = ctypes.c_int64()
+        _lib.check(self._L.nufft3d_plan_footprint(self.plan, int(nc), int(bool(with_solver)), ctypes.byref(b)))
+        return int(b.value)
 
     @property
     def plan(self):
@@ -232,6 +249,7 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
         t._adjoint = not self._adjoint
         t._owner = self  # keep the plan alive
         t._plan = self._plan
+        t._borrowed = True
         return t
 
     def mtimes(self, x):

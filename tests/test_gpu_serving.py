@@ -1,0 +1,108 @@
+"""GPU tests of shared plan handles and the continuous-batching server.
+
+Isolation: each request's reconstruction through the server -- concurrent
+with other requests, possibly merged with same-trajectory requests into one
+multi-coil solve -- equals the same request solved alone, within the
+iterative-image tolerance (rel L2 <= 1e-4).
+"""
+import threading
+
+import numpy as np
+import pytest
+
+from nufft_3d_gb300 import nufft_3d, synth
+from nufft_3d_gb300.serving import ReconServer, Request, run_plain, run_served, summarize
+
+pytestmark = pytest.mark.gpu
+TOL_IMG = 1e-4
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def make_request(N, n_spokes, nc, seed, arrival=0.0, traj_seed=None):
+    rng = np.random.default_rng(seed)
+    om = synth.koosh_ball(N, N, n_spokes)
+    if traj_seed is not None:  # a different trajectory: rotate the sphere
+        a = np.random.default_rng(traj_seed).uniform(0, 2 * np.pi)
+        R = np.array([[np.cos(a), -np.sin(a), 0], [np.sin(a), np.cos(a), 0], [0, 0, 1]])
+        om = R @ om
+    raw = (rng.standard_normal((om.shape[1], nc)) + 1j * rng.standard_normal((om.shape[1], nc))).astype(np.complex64)
+    return Request(om=om, N=N, raw=raw, maxit=10, damp=0.05, arrival=arrival)
+
+
+def test_shared_handles_run_concurrently(cuda):
+    req = make_request(32, 800, 2, 0)
+    base = nufft_3d(req.om, req.N, "J", 6)
+    alone = base.iNUFT(req.raw, 10, 0.05, solver="cg", tol=0)
+    handles = [base.share() for _ in range(3)]
+    out = [None] * 3
+
+    def run(i):
+        out[i] = handles[i].iNUFT(req.raw, 10, 0.05, solver="cg", tol=0)
+
+    th = [threading.Thread(target=run, args=(i,)) for i in range(3)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for o in out:
+        assert rel(o, alone) < TOL_IMG
+    base.close()  # tables stay alive while handles exist
+    assert rel(handles[0].iNUFT(req.raw, 10, 0.05, solver="cg", tol=0), alone) < TOL_IMG
+    for h in handles:
+        h.close()
+
+
+def test_server_results_match_alone(cuda):
+    reqs = [make_request(32, 600, 2, 1, traj_seed=1), make_request(48, 900, 3, 2, traj_seed=2),
+            make_request(32, 600, 1, 3, traj_seed=1), make_request(24, 500, 4, 4, traj_seed=3),
+            make_request(32, 600, 2, 5, traj_seed=1)]
+    alone = []
+    for r in reqs:
+        obj = nufft_3d(r.om, r.N, **r.opts)
+        alone.append(obj.iNUFT(r.raw, r.maxit, r.damp, solver=r.solver, tol=r.tol))
+        obj.close()
+    srv = ReconServer(slots=3, max_batch_coils=8)
+    futs = [srv.submit(r) for r in reqs]   # all queued at once: same-trajectory ones merge
+    done = [f.result(timeout=120) for f in futs]
+    srv.close()
+    assert not srv.errors
+    for r, a in zip(done, alone):
+        assert r.result.shape == a.shape
+        assert rel(r.result, a) < TOL_IMG
+
+
+def test_server_admission_small_budget(cuda):
+    reqs = [make_request(32, 600, 2, s, traj_seed=s) for s in range(4)]
+    one = ReconServer._work_bytes(reqs[0], 2) + ReconServer._plan_bytes_estimate(reqs[0])
+    srv = ReconServer(slots=4, hbm_budget=int(one * 1.5))   # room for one batch at a time
+    peak = [0]
+    orig = srv._admit
+
+    def admit(slot):
+        job = orig(slot)
+        peak[0] = max(peak[0], srv.used)
+        return job
+
+    srv._admit = admit
+    futs = [srv.submit(r) for r in reqs]
+    done = [f.result(timeout=120) for f in futs]
+    srv.close()
+    assert not srv.errors and len(done) == 4
+    assert peak[0] <= srv.budget
+
+
+def test_served_vs_plain_stream(cuda):
+    reqs = []
+    for i in range(8):
+        reqs.append(make_request(32, 600, 2, 10 + i, arrival=0.01 * i, traj_seed=i % 2))
+    served, wall_s = run_served([Request(**{k: getattr(r, k) for k in ("om", "N", "raw", "maxit", "damp", "arrival")})
+                                 for r in reqs], slots=3)
+    plain, wall_p = run_plain(reqs)
+    for a, b in zip(sorted(served, key=lambda r: r.arrival), sorted(plain, key=lambda r: r.arrival)):
+        assert rel(a.result, b.result) < TOL_IMG
+    s = summarize(served, wall_s)
+    p = summarize(plain, wall_p)
+    assert s["requests"] == p["requests"] == 8
