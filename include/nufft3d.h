@@ -164,6 +164,25 @@ int nufft3d_inverse_host(nufft3d_plan *plan, const float *raw_host, float *x_hos
                          int maxit, double damp, const float *W_host, int solver,
                          double tol, int *iters_host);
 
+/* ---- Batches: many volumes (different N, trajectories, coil counts) per launch.
+ * No single counterpart in the reference, which handles one object at a time;
+ * each volume's result equals what fNUFT / aNUFT / iNUFT of its own plan
+ * gives.  plans[v] must be distinct handles (nufft3d_plan_share for repeated
+ * trajectories) sharing ceil(J/2), the kernel type and 2-D/3-D; the batch uses
+ * their work buffers, so do not use those handles concurrently with it. */
+typedef struct nufft3d_batch nufft3d_batch;
+int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, int nvol, nufft3d_batch **batch);
+int nufft3d_batch_destroy(nufft3d_batch *batch);
+/* x_dev[v] [N1 N2 N3 nc_v] -> k_dev[v] [M_v nc_v] for every volume, one launch per stage. */
+int nufft3d_batch_forward(nufft3d_batch *batch, const float *const *x_dev, float *const *k_dev, void *stream);
+/* k_dev[v] -> x_dev[v] for every volume. */
+int nufft3d_batch_adjoint(nufft3d_batch *batch, const float *const *k_dev, float *const *x_dev, void *stream);
+/* iNUFT of every (volume, coil) system with conjugate gradients, W = d, x0 = 0
+ * (iNUFT.m:119-136 with the CG solver), FP64 scalars; iters_host
+ * (optional) receives the iteration count of each system, volume-major. */
+int nufft3d_batch_inverse(nufft3d_batch *batch, const float *const *raw_dev, float *const *x_dev, int maxit,
+                          double damp, double tol, int *iters_host, void *stream);
+
 /* Re-runs density.m on the plan (maxit iterations) and stores it as obj.d. */
 int nufft3d_density(nufft3d_plan *plan, int maxit);
 

@@ -74,6 +74,11 @@ SIGNATURES = {
     "nufft3d_inverse_host": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_double, _P,
                                             ctypes.c_int, ctypes.c_double, _P]),
     "nufft3d_density": (ctypes.c_int, [_P, ctypes.c_int]),
+    "nufft3d_batch_create": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "nufft3d_batch_destroy": (ctypes.c_int, [_P]),
+    "nufft3d_batch_forward": (ctypes.c_int, [_P, _P, _P, _P]),
+    "nufft3d_batch_adjoint": (ctypes.c_int, [_P, _P, _P, _P]),
+    "nufft3d_batch_inverse": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, _P, _P]),
     "nufft3d_profile": (ctypes.c_int, [_P, ctypes.c_int]),
     "nufft3d_profile_read": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int]),
     "nufft3d_last_error": (ctypes.c_char_p, []),

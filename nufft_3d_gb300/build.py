@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnufft3d.so")
-SOURCES = ["plan.cu", "api.cu", "fft.cu", "interp.cu", "solver.cu", "noalloc.cu"]
+SOURCES = ["plan.cu", "api.cu", "fft.cu", "interp.cu", "solver.cu", "noalloc.cu", "batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unused-function"]

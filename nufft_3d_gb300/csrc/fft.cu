@@ -189,7 +189,7 @@ __device__ float2 *block_fft(float2 *a, float2 *b, int nlines, int LS, const FFT
     return a;
 }
 
-static bool needs_rare(const FFTDesc &f)
+bool needs_rare(const FFTDesc &f)
 {
     for (int s = 0; s < f.nst; ++s)
         if (f.rad[s] == 7 || f.rad[s] == 11 || f.rad[s] == 13) return true;
@@ -209,14 +209,12 @@ constexpr int kMaxLineCoils = 16;
 // FX: image (user layout) * U -> B1, length-K1 FFT along x for one (y,z) line
 // of up to kMaxLineCoils coils.  fNUFT.m:5 + nufft_3d.m:287-289 (j=1).
 template <bool RARE>
-__global__ void __launch_bounds__(kFftThreads)
-k_fx(const float2 *__restrict__ img, const float *__restrict__ U, float2 *__restrict__ B1,
-     int N1, int N23, int nc, FFTDesc fd)
+__device__ __forceinline__ void fx_body(const float2 *__restrict__ img, const float *__restrict__ U,
+                                        float2 *__restrict__ B1, int N1, int N23, int nc,
+                                        const FFTDesc &fd, int line, int cchunk, float2 *sm)
 {
-    extern __shared__ float2 sm[];
     const int K = fd.n, LS = K + 1;
-    const int line = blockIdx.x;
-    const int c0 = blockIdx.y * kMaxLineCoils;
+    const int c0 = cchunk * kMaxLineCoils;
     const int nv = min(kMaxLineCoils, nc - c0);
     float2 *A = sm, *B = sm + nv * LS;
     const int nz = K - N1;
@@ -240,18 +238,25 @@ k_fx(const float2 *__restrict__ img, const float *__restrict__ U, float2 *__rest
     }
 }
 
+template <bool RARE>
+__global__ void __launch_bounds__(kFftThreads)
+k_fx(const float2 *__restrict__ img, const float *__restrict__ U, float2 *__restrict__ B1,
+     int N1, int N23, int nc, FFTDesc fd)
+{
+    extern __shared__ float2 sm[];
+    fx_body<RARE>(img, U, B1, N1, N23, nc, fd, blockIdx.x, blockIdx.y, sm);
+}
+
 // IX: B1 -> image, unnormalised inverse FFT along x, crop, *U*scale
 // (+ add_coef * addend).  nufft_3d.m:296-298 (j=1) + aNUFT.m:8-9.
 template <bool RARE>
-__global__ void __launch_bounds__(kFftThreads)
-k_ix(const float2 *__restrict__ B1, const float *__restrict__ U, float2 *__restrict__ img,
-     int N1, int N23, int nc, FFTDesc fd, float scale, const float2 *__restrict__ addend,
-     float add_coef)
+__device__ __forceinline__ void ix_body(const float2 *__restrict__ B1, const float *__restrict__ U,
+                                        float2 *__restrict__ img, int N1, int N23, int nc,
+                                        const FFTDesc &fd, float scale, const float2 *__restrict__ addend,
+                                        float add_coef, int line, int cchunk, float2 *sm)
 {
-    extern __shared__ float2 sm[];
     const int K = fd.n, LS = K + 1;
-    const int line = blockIdx.x;
-    const int c0 = blockIdx.y * kMaxLineCoils;
+    const int c0 = cchunk * kMaxLineCoils;
     const int nv = min(kMaxLineCoils, nc - c0);
     float2 *A = sm, *B = sm + nv * LS;
     const float2 *ib = B1 + (size_t)line * K * nc + c0;
@@ -278,16 +283,26 @@ k_ix(const float2 *__restrict__ B1, const float *__restrict__ U, float2 *__restr
     }
 }
 
-// Strided pass along y or z over rows of contiguous complex vectors.
 template <bool RARE>
 __global__ void __launch_bounds__(kFftThreads)
-k_line(const float2 *__restrict__ in, float2 *__restrict__ out, LinePass lp, FFTDesc fd, int inv)
+k_ix(const float2 *__restrict__ B1, const float *__restrict__ U, float2 *__restrict__ img,
+     int N1, int N23, int nc, FFTDesc fd, float scale, const float2 *__restrict__ addend,
+     float add_coef)
 {
     extern __shared__ float2 sm[];
+    ix_body<RARE>(B1, U, img, N1, N23, nc, fd, scale, addend, add_coef, blockIdx.x, blockIdx.y, sm);
+}
+
+// Strided pass along y or z over rows of contiguous complex vectors.
+template <bool RARE>
+__device__ __forceinline__ void line_body(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                          const LinePass &lp, const FFTDesc &fd, int inv, int blk,
+                                          float2 *sm)
+{
     const int K = fd.n, LS = K + 1, vec = lp.vec;
     float2 *A = sm, *B = sm + vec * LS;
-    const int outer = blockIdx.x / lp.nchunks;
-    const int chunk = blockIdx.x - outer * lp.nchunks;
+    const int outer = blk / lp.nchunks;
+    const int chunk = blk - outer * lp.nchunks;
     const float2 *ib = in + outer * lp.in_outer_stride + (int64_t)chunk * vec;
     float2 *ob = out + outer * lp.out_outer_stride + (int64_t)chunk * vec;
     const float sg = inv ? -1.f : 1.f;
@@ -314,6 +329,14 @@ k_line(const float2 *__restrict__ in, float2 *__restrict__ out, LinePass lp, FFT
     }
 }
 
+template <bool RARE>
+__global__ void __launch_bounds__(kFftThreads)
+k_line(const float2 *__restrict__ in, float2 *__restrict__ out, LinePass lp, FFTDesc fd, int inv)
+{
+    extern __shared__ float2 sm[];
+    line_body<RARE>(in, out, lp, fd, inv, blockIdx.x, sm);
+}
+
 // ----------------------------------------------------------------- host
 bool fft_factor(int n, FFTDesc &d)
 {
@@ -331,7 +354,7 @@ bool fft_factor(int n, FFTDesc &d)
     return m == 1;
 }
 
-static int line_vec(int64_t rowlen)
+int line_vec(int64_t rowlen)
 {
     const int cands[] = {16, 8, 4, 2, 1};
     for (int v : cands)
@@ -339,12 +362,10 @@ static int line_vec(int64_t rowlen)
     return 1;
 }
 
-static size_t line_smem(int vec, int K) { return (size_t)2 * vec * (K + 1) * sizeof(float2); }
+size_t line_smem(int vec, int K) { return (size_t)2 * vec * (K + 1) * sizeof(float2); }
 
-static int launch_line(const float2 *in, float2 *out, int n_outer, int64_t rowlen,
-                       int n_in, int n_out, int Nimg, int pad_in, int crop_out,
-                       int64_t in_axis, int64_t out_axis, int64_t in_outer, int64_t out_outer,
-                       const FFTDesc &fd, int inv, cudaStream_t s)
+LinePass make_linepass(int n_outer, int64_t rowlen, int n_in, int n_out, int Nimg, int pad_in, int crop_out,
+                       int64_t in_axis, int64_t out_axis, int64_t in_outer, int64_t out_outer, int64_t *nblk)
 {
     LinePass lp;
     lp.vec = line_vec(rowlen);
@@ -358,13 +379,54 @@ static int launch_line(const float2 *in, float2 *out, int n_outer, int64_t rowle
     lp.out_axis_stride = out_axis;
     lp.in_outer_stride = in_outer;
     lp.out_outer_stride = out_outer;
-    const int64_t nblk = (int64_t)n_outer * lp.nchunks;
+    *nblk = (int64_t)n_outer * lp.nchunks;
+    return lp;
+}
+
+static int launch_line(const float2 *in, float2 *out, int n_outer, int64_t rowlen,
+                       int n_in, int n_out, int Nimg, int pad_in, int crop_out,
+                       int64_t in_axis, int64_t out_axis, int64_t in_outer, int64_t out_outer,
+                       const FFTDesc &fd, int inv, cudaStream_t s)
+{
+    int64_t nblk = 0;
+    const LinePass lp = make_linepass(n_outer, rowlen, n_in, n_out, Nimg, pad_in, crop_out, in_axis, out_axis,
+                                      in_outer, out_outer, &nblk);
     if (nblk <= 0) return NUFFT3D_SUCCESS;
     if (nblk > 0x7fffffff) return fail(NUFFT3D_ERR_SIZE, "FFT pass grid too large");
     if (needs_rare(fd))
         k_line<true><<<(unsigned)nblk, kFftThreads, line_smem(lp.vec, fd.n), s>>>(in, out, lp, fd, inv);
     else
         k_line<false><<<(unsigned)nblk, kFftThreads, line_smem(lp.vec, fd.n), s>>>(in, out, lp, fd, inv);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
+// Batched passes over many volumes in one launch: block -> (volume, index,
+// coil chunk) from `table`; kind 0 = x pass forward, 1 = strided pass,
+// 2 = x pass adjoint.
+template <bool RARE>
+__global__ void __launch_bounds__(kFftThreads)
+k_fft_batch(const BatchFFT *__restrict__ vols, const int4 *__restrict__ table, int kind)
+{
+    extern __shared__ float2 sm[];
+    const int4 e = table[blockIdx.x];
+    const BatchFFT &b = vols[e.x];
+    if (kind == 0)
+        fx_body<RARE>(b.in, b.U, b.out, b.N1, b.N23, b.nc, b.fd, e.y, e.z, sm);
+    else if (kind == 1)
+        line_body<RARE>(b.in, b.out, b.lp, b.fd, b.inv, e.y, sm);
+    else
+        ix_body<RARE>(b.in, b.U, b.out, b.N1, b.N23, b.nc, b.fd, b.scale, b.addend, b.add_coef, e.y, e.z, sm);
+}
+
+int launch_fft_batch(const BatchFFT *vols, const int4 *table, int nblocks, int kind, size_t smem, bool rare,
+                     cudaStream_t s)
+{
+    if (nblocks <= 0) return NUFFT3D_SUCCESS;
+    if (rare)
+        k_fft_batch<true><<<nblocks, kFftThreads, smem, s>>>(vols, table, kind);
+    else
+        k_fft_batch<false><<<nblocks, kFftThreads, smem, s>>>(vols, table, kind);
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }
@@ -445,6 +507,8 @@ int configure_fft_kernels()
     NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fx<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
     NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_ix<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
     NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fft_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fft_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
     return NUFFT3D_SUCCESS;
 }
 

@@ -116,6 +116,55 @@ struct LinePass {
     int64_t in_axis_stride, out_axis_stride, in_outer_stride, out_outer_stride;
 };
 
+// ------------------------------------------------------- batched stages
+// One descriptor per volume and stage for the batched (multi-volume) launches.
+struct BatchFFT {
+    const float2 *in;
+    float2 *out;
+    const float *U;
+    const float2 *addend;
+    int N1, N23, nc, inv;
+    float scale, add_coef;
+    LinePass lp;
+    FFTDesc fd;
+};
+
+struct BatchInterp {
+    const float2 *in;   // gather: grid; spread: sorted samples
+    float2 *out;        // gather: sorted samples; spread: grid
+    const float4 *samples;
+    const int4 *blocks;
+    const float *wsample;
+    Geom g;
+    KBParams kb;
+    const int *cand;
+    int n_cand;
+    int nc;
+    float scale;
+};
+
+struct BatchPerm {
+    const float2 *in;
+    float2 *out;
+    const int32_t *inv;
+    const float *w;     // permute_in weights (sorted order) or null
+    int64_t M;
+    int nc;
+    float scale;
+};
+
+LinePass make_linepass(int n_outer, int64_t rowlen, int n_in, int n_out, int Nimg, int pad_in, int crop_out,
+                       int64_t in_axis, int64_t out_axis, int64_t in_outer, int64_t out_outer, int64_t *nblk);
+int line_vec(int64_t rowlen);
+size_t line_smem(int vec, int K);
+bool needs_rare(const FFTDesc &f);
+constexpr int kMaxLineCoilsHost = 16;
+int launch_fft_batch(const BatchFFT *vols, const int4 *table, int nblocks, int kind, size_t smem, bool rare,
+                     cudaStream_t s);
+int launch_interp_batch(bool gather, int cb, int R, bool radial, const BatchInterp *vols, const int4 *table,
+                        int nblocks, size_t smem, cudaStream_t s);
+int launch_perm_batch(bool out, const BatchPerm *vols, const int4 *table, int nblocks, cudaStream_t s);
+
 // ----------------------------------------------------------------- plan
 struct Scratch {
     int nc = 0;
@@ -246,6 +295,8 @@ int prepare_weights(nufft3d_plan *p, const float *W_orig, const float **wsorted,
 int refresh_density_orig(nufft3d_plan *p, cudaStream_t s);
 
 int run_density(nufft3d_plan *p, int maxit, cudaStream_t s);
+// iNUFT work vectors of a plan handle for nc coils (r, p, q, v, vprev, w1, w2, scalars)
+int ensure_solver(nufft3d_plan *p, int nc);
 int run_inverse(nufft3d_plan *p, const float2 *raw, float2 *x, int nc, int maxit,
                 double damp, const float *W_orig, int solver, double tol, int *iters_host,
                 cudaStream_t s);

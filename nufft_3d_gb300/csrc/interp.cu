@@ -185,19 +185,17 @@ __device__ __forceinline__ int eval_chunk(int base, const SampleGeo &sg, const C
 // Gather: tile staged coil-major ([CB][P^3] complex) -> ks.  kGroup lanes per
 // sample walk the candidate list; partial sums are reduced across the group.
 template <int CB, bool RADIAL, int R>
-__global__ void __launch_bounds__(kInterpThreads)
-k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
-         const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
-         KBParams kb, float scale, const float *__restrict__ wsample, Cand cd)
+__device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
+                                            const float4 *__restrict__ samples, const int4 bi, const Geom &g,
+                                            const KBParams &kb, float scale, const float *__restrict__ wsample,
+                                            const Cand &cd, float4 *smem4)
 {
-    extern __shared__ float4 smem4[];
     constexpr int pv = Plane<R>::PS;
     const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
     CandSmem cs;
     cs.f = smem4;
     cs.off = reinterpret_cast<int *>(smem4 + cd.n);
     float2 *tile = reinterpret_cast<float2 *>(cs.off + 8 * cd.n);
-    const int4 bi = blocks[blockIdx.x];
     const int tid = bi.x;
     const int tx = tid % g.nt[0];
     const int ty = (tid / g.nt[0]) % g.nt[1];
@@ -271,6 +269,16 @@ k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
     }
 }
 
+template <int CB, bool RADIAL, int R>
+__global__ void __launch_bounds__(kInterpThreads)
+k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
+         const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
+         KBParams kb, float scale, const float *__restrict__ wsample, Cand cd)
+{
+    extern __shared__ float4 smem4[];
+    gather_body<CB, RADIAL, R>(G, ks, nc, c0, samples, blocks[blockIdx.x], g, kb, scale, wsample, cd, smem4);
+}
+
 // Spread: ks -> tile -> grid.  The tile accumulates in 32-bit fixed point
 // with native shared-memory integer reductions (floating-point shared atomics
 // are several times slower on this part).  Per block and call the scale is a
@@ -318,22 +326,18 @@ struct IPlane {
 };
 
 template <int CB, bool RADIAL, int R>
-__global__ void __launch_bounds__(kInterpThreads)
-k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
-         const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
-         KBParams kb, Cand cd)
+__device__ __forceinline__ void spread_body(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
+                                            const float4 *__restrict__ samples, const int4 bi, const Geom &g,
+                                            const KBParams &kb, const Cand &cd, float4 *smem4, float *red,
+                                            TapQueue *queues)
 {
     constexpr int NP = Lanes<CB>::NP, CPS = Lanes<CB>::CPS;
     constexpr int ps = IPlane<R>::PS;
-    extern __shared__ float4 smem4[];
-    __shared__ float red[33];
-    __shared__ TapQueue queues[kInterpThreads / 32];
     const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
     CandSmem cs;
     cs.f = smem4;
     cs.off = reinterpret_cast<int *>(smem4 + cd.n);
     int *tile = reinterpret_cast<int *>(smem4 + cd.n + 2 * cd.n);
-    const int4 bi = blocks[blockIdx.x];
     const int tid = bi.x;
     const int tx = tid % g.nt[0];
     const int ty = (tid / g.nt[0]) % g.nt[1];
@@ -419,6 +423,18 @@ k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
     }
 }
 
+template <int CB, bool RADIAL, int R>
+__global__ void __launch_bounds__(kInterpThreads)
+k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
+         const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
+         KBParams kb, Cand cd)
+{
+    extern __shared__ float4 smem4[];
+    __shared__ float red[33];
+    __shared__ TapQueue queues[kInterpThreads / 32];
+    spread_body<CB, RADIAL, R>(ks, G, nc, c0, samples, blocks[blockIdx.x], g, kb, cd, smem4, red, queues);
+}
+
 // Plan-time bound for the fixed-point spread: for each block, the largest
 // sum of kernel weights its samples put on one tile point (float shared
 // atomics; runs once per plan).  Written to blocks[b].w as float bits.
@@ -489,6 +505,63 @@ __global__ void k_permute_in(const float2 *__restrict__ k, float2 *__restrict__ 
     for (int c = 0; c < nc; ++c) {
         float2 v = k[m + M * c];
         ks[(size_t)s * nc + c] = make_float2(v.x * w, v.y * w);
+    }
+}
+
+// Batched interpolation: block -> (volume, tile piece, first coil) from
+// `table`; one launch covers every volume of a batch.
+template <int CB, bool RADIAL, int R>
+__global__ void __launch_bounds__(kInterpThreads)
+k_gather_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ table)
+{
+    extern __shared__ float4 smem4[];
+    const int4 e = table[blockIdx.x];
+    const BatchInterp &b = vols[e.x];
+    const Cand cd{b.cand, b.n_cand};
+    gather_body<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, b.kb, b.scale, b.wsample,
+                               cd, smem4);
+}
+
+template <int CB, bool RADIAL, int R>
+__global__ void __launch_bounds__(kInterpThreads)
+k_spread_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ table)
+{
+    extern __shared__ float4 smem4[];
+    __shared__ float red[33];
+    __shared__ TapQueue queues[kInterpThreads / 32];
+    const int4 e = table[blockIdx.x];
+    const BatchInterp &b = vols[e.x];
+    const Cand cd{b.cand, b.n_cand};
+    spread_body<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, b.kb, cd, smem4, red,
+                               queues);
+}
+
+// Batched permutes: block -> (volume, chunk of 256 samples).
+__global__ void k_perm_batch(const BatchPerm *__restrict__ vols, const int4 *__restrict__ table, int out)
+{
+    const int4 e = table[blockIdx.x];
+    const BatchPerm &b = vols[e.x];
+    const int64_t m = (int64_t)e.y * blockDim.x + threadIdx.x;
+    if (m >= b.M) return;
+    const int s = b.inv[m];
+    const int nc = b.nc;
+    if (out) {
+        for (int c = 0; c < nc; ++c) {
+            float2 v = make_float2(0.f, 0.f);
+            if (s >= 0) {
+                v = b.in[(size_t)s * nc + c];
+                v.x *= b.scale;
+                v.y *= b.scale;
+            }
+            b.out[m + b.M * c] = v;
+        }
+    } else {
+        if (s < 0) return;
+        const float w = b.w ? b.w[s] : 1.f;
+        for (int c = 0; c < nc; ++c) {
+            const float2 v = b.in[m + b.M * c];
+            b.out[(size_t)s * nc + c] = make_float2(v.x * w, v.y * w);
+        }
     }
 }
 
@@ -629,6 +702,53 @@ int launch_permute_in(nufft3d_plan *p, const float2 *k, float2 *ks, int nc,
     return NUFFT3D_SUCCESS;
 }
 
+
+template <int CB, bool RADIAL, int R>
+static int interp_batch_t(bool gather, const BatchInterp *vols, const int4 *table, int nblocks, size_t smem,
+                          cudaStream_t s)
+{
+    if (gather)
+        k_gather_batch<CB, RADIAL, R><<<nblocks, kInterpThreads, smem, s>>>(vols, table);
+    else
+        k_spread_batch<CB, RADIAL, R><<<nblocks, kInterpThreads, smem, s>>>(vols, table);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
+template <int CB, bool RADIAL>
+static int interp_batch_r(bool gather, int R, const BatchInterp *vols, const int4 *table, int nblocks, size_t smem,
+                          cudaStream_t s)
+{
+    switch (R) {
+    case 1: return interp_batch_t<CB, RADIAL, 1>(gather, vols, table, nblocks, smem, s);
+    case 2: return interp_batch_t<CB, RADIAL, 2>(gather, vols, table, nblocks, smem, s);
+    case 3: return interp_batch_t<CB, RADIAL, 3>(gather, vols, table, nblocks, smem, s);
+    default: return interp_batch_t<(CB < 8 ? CB : 4), RADIAL, 4>(gather, vols, table, nblocks, smem, s);
+    }
+}
+
+int launch_interp_batch(bool gather, int cb, int R, bool radial, const BatchInterp *vols, const int4 *table,
+                        int nblocks, size_t smem, cudaStream_t s)
+{
+    if (nblocks <= 0) return NUFFT3D_SUCCESS;
+    if (cb >= 8) return radial ? interp_batch_r<8, true>(gather, R, vols, table, nblocks, smem, s)
+                               : interp_batch_r<8, false>(gather, R, vols, table, nblocks, smem, s);
+    if (cb >= 4) return radial ? interp_batch_r<4, true>(gather, R, vols, table, nblocks, smem, s)
+                               : interp_batch_r<4, false>(gather, R, vols, table, nblocks, smem, s);
+    if (cb >= 2) return radial ? interp_batch_r<2, true>(gather, R, vols, table, nblocks, smem, s)
+                               : interp_batch_r<2, false>(gather, R, vols, table, nblocks, smem, s);
+    return radial ? interp_batch_r<1, true>(gather, R, vols, table, nblocks, smem, s)
+                  : interp_batch_r<1, false>(gather, R, vols, table, nblocks, smem, s);
+}
+
+int launch_perm_batch(bool out, const BatchPerm *vols, const int4 *table, int nblocks, cudaStream_t s)
+{
+    if (nblocks <= 0) return NUFFT3D_SUCCESS;
+    k_perm_batch<<<nblocks, 256, 0, s>>>(vols, table, out ? 1 : 0);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
 // Allow each kernel all the shared memory a block can have, less its static part.
 template <typename K>
 static int allow_smem(K kernel)
@@ -645,6 +765,8 @@ static int cfg_one()
 {
     NUFFT_TRY(allow_smem(k_gather<CB, RADIAL, R>));
     NUFFT_TRY(allow_smem(k_spread<CB, RADIAL, R>));
+    NUFFT_TRY(allow_smem(k_gather_batch<CB, RADIAL, R>));
+    NUFFT_TRY(allow_smem(k_spread_batch<CB, RADIAL, R>));
     return NUFFT3D_SUCCESS;
 }
 

@@ -326,7 +326,7 @@ int prepare_weights(nufft3d_plan *p, const float *W_orig, const float **wsorted,
     return NUFFT3D_SUCCESS;
 }
 
-static int ensure_solver(nufft3d_plan *p, int nc)
+int ensure_solver(nufft3d_plan *p, int nc)
 {
     SolverWork &w = p->solver;
     const size_t nimg = (size_t)p->N[0] * p->N[1] * p->N[2];
