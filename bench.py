@@ -165,6 +165,120 @@ def build_inputs(N, n_read, n_spokes, nc):
     return om, im.astype(np.complex64)
 
 
+def rotated(om, seed):
+    """The same trajectory shape under a seeded random rotation (a new trajectory)."""
+    rng = np.random.default_rng(seed)
+    q = rng.standard_normal(4)
+    q /= np.linalg.norm(q)
+    a, b, c, d = q
+    R = np.array([[a * a + b * b - c * c - d * d, 2 * (b * c - a * d), 2 * (b * d + a * c)],
+                  [2 * (b * c + a * d), a * a - b * b + c * c - d * d, 2 * (c * d - a * b)],
+                  [2 * (b * d - a * c), 2 * (c * d + a * b), a * a - b * b - c * c + d * d]])
+    return R @ om
+
+
+def config3_volumes(n_vol=48, seed=3):
+    """Batched uneven sizes: N in {64, 96, 128, 160}, radial / stack-of-spirals /
+    uniform-random trajectories (0.5-1.5 N^3 samples), 4-16 coils each."""
+    from nufft_3d_gb300 import synth
+    rng = np.random.default_rng(seed)
+    vols = []
+    for v in range(n_vol):
+        N = int(rng.choice([64, 96, 128, 160]))
+        kind = ["radial", "spiral", "random"][v % 3]
+        nc = int(rng.integers(4, 17))
+        count = int(rng.uniform(0.5, 1.5) * N ** 3)
+        if kind == "radial":
+            om = rotated(synth.koosh_ball(N, N, max(1, count // N)), seed + v)
+        elif kind == "spiral":
+            parts = min(64, N)
+            om = synth.stack_of_spirals(N, n_interleaves=16, n_samples=max(64, count // (16 * parts)),
+                                        n_partitions=parts)
+        else:
+            om = synth.random_uniform(N, count, seed=seed + v)
+        vols.append((om, N, nc, kind))
+    return vols
+
+
+def bench_batched(maxit=20, damp=1e-3):
+    """Config 3: 48 uneven volumes reconstructed by the batched CG (one launch per
+    stage for all volumes) against the same volumes one after another."""
+    import torch
+    from nufft_3d_gb300 import NufftBatch, nufft_3d
+    vols = config3_volumes()
+    objs = [nufft_3d(om, N, "J", 6, density_iters=20) for om, N, _, _ in vols]
+    ncs = [nc for _, _, nc, _ in vols]
+    g = torch.Generator(device="cuda").manual_seed(0)
+    raws = [torch.randn((nc, o.M), dtype=torch.complex64, device="cuda", generator=g) for o, nc in zip(objs, ncs)]
+    batch = NufftBatch(objs, ncs)
+    batch.inverse(raws, 2, damp)            # warm-up (graph, buffers)
+    for o, r in zip(objs, raws):
+        o.iNUFT(r, 2, damp, solver="cg", tol=0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    xb = batch.inverse(raws, maxit, damp)
+    torch.cuda.synchronize()
+    t_b = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    xs = [o.iNUFT(r, maxit, damp, solver="cg", tol=0) for o, r in zip(objs, raws)]
+    torch.cuda.synchronize()
+    t_s = time.perf_counter() - t0
+    err = max(float((a - b).abs().norm() / b.abs().norm()) for a, b in zip(xb, xs))
+    samples = sum(o.M * nc for o, nc in zip(objs, ncs))
+    batch.close()
+    for o in objs:
+        o.close()
+    return {"workload": "config3: 48 volumes, N in {64,96,128,160}, radial/spiral/random, 4-16 coils, "
+                        "%d CG iterations, damp %g" % (maxit, damp),
+            "coil_samples": samples, "batched_volumes_per_s": round(len(vols) / t_b, 3),
+            "sequential_volumes_per_s": round(len(vols) / t_s, 3), "speedup": round(t_s / t_b, 3),
+            "batched_s": round(t_b, 3), "sequential_s": round(t_s, 3),
+            "max_rel_l2_batched_vs_single": err}
+
+
+def serving_requests(n_req=40, rate=20.0, seed=5):
+    """Config 5 stream: Poisson arrivals; 60% reuse one of 8 resident trajectories,
+    40% new ones; shapes from the config-2/3 mixes; 20 CG iterations each."""
+    from nufft_3d_gb300 import synth
+    from nufft_3d_gb300.serving import Request
+    rng = np.random.default_rng(seed)
+    shapes = [(64, 64, 2048, 4), (96, 96, 4096, 6), (128, 128, 8192, 8), (64, 64, 4096, 8)]
+    resident = []
+    for i in range(8):
+        N, nr, ns, nc = shapes[i % len(shapes)]
+        resident.append((rotated(synth.koosh_ball(N, nr, ns), 100 + i), N, nc))
+    reqs = []
+    t = 0.0
+    for i in range(n_req):
+        t += rng.exponential(1.0 / rate)
+        if rng.random() < 0.6:
+            om, N, nc = resident[int(rng.integers(0, 8))]
+        else:
+            N, nr, ns, nc = shapes[int(rng.integers(0, len(shapes)))]
+            om = rotated(synth.koosh_ball(N, nr, ns), 1000 + i)
+        raw = (rng.standard_normal((om.shape[1], nc)) + 1j * rng.standard_normal((om.shape[1], nc))).astype(np.complex64)
+        reqs.append(Request(om=om, N=N, raw=raw, maxit=20, damp=1e-3, arrival=t))
+    return reqs
+
+
+def bench_serving(slots=4):
+    from nufft_3d_gb300.serving import Request, run_plain, run_served, summarize
+    reqs = serving_requests()
+    copy = [Request(om=r.om, N=r.N, raw=r.raw, maxit=r.maxit, damp=r.damp, arrival=r.arrival, key=r.key)
+            for r in reqs]
+    served, wall_s = run_served(reqs, slots=slots)
+    plain, wall_p = run_plain(copy)
+    err = max(float(np.linalg.norm(a.result - b.result) / np.linalg.norm(b.result))
+              for a, b in zip(served, sorted(plain, key=lambda r: r.arrival)))
+    s = summarize(served, wall_s)
+    p = summarize(plain, wall_p)
+    return {"workload": "config5: %d requests, Poisson 20 req/s, 60%% on 8 resident trajectories, "
+                        "N in {64,96,128}, 4-8 coils, 20 CG iterations" % len(reqs),
+            "served": s, "plain": p, "throughput_speedup": round(s["volumes_per_s"] / p["volumes_per_s"], 3),
+            "p50_speedup": round(p["p50_ms"] / s["p50_ms"], 3), "slots": slots,
+            "max_rel_l2_served_vs_plain": err}
+
+
 def cpu_baseline(om, N, n_read, nc, steps=3):
     from oracle import cpu_bench
     return cpu_bench.run(om, N, n_read, nc, steps)
@@ -201,6 +315,7 @@ def main():
     ap.add_argument("--n-spokes", dest="n_spokes", type=int, default=32768)
     ap.add_argument("--nc", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched (config 3) and serving (config 5) runs")
     ap.add_argument("--tile", type=str, default=None)
     ap.add_argument("--coils-per-pass", type=int, default=0)
     ap.add_argument("--samples-per-block", type=int, default=0)
@@ -312,6 +427,12 @@ def main():
             "roofline": roof,
             "stages": stages,
             "clocks": clk.summary()}
+    if not args.no_extras and ws == 1:
+        obj.close()
+        del x, k, x2, xh, kh, x2h
+        torch.cuda.empty_cache()
+        line["batched"] = bench_batched()
+        line["serving"] = bench_serving()
     if not args.no_cpu_baseline and ws == 1:
         line["cpu_baseline"] = cpu_baseline(om, args.N, args.n_read, nc)
     print(json.dumps(line))

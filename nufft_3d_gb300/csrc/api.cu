@@ -29,6 +29,7 @@ int ensure_scratch(nufft3d_plan *p, int nc)
 {
     Scratch &s = p->scratch;
     if (s.nc >= nc) return NUFFT3D_SUCCESS;
+    NUFFT_DEVICE_LOCK;
     const Geom &g = p->geom;
     const size_t K1 = g.K[0], K2 = g.K[1], K3 = g.K[2];
     const size_t N2 = p->N[1], N3 = p->N[2];
@@ -316,6 +317,7 @@ int run_density(nufft3d_plan *p, int maxit, cudaStream_t s)
     // density.m:42: d = d / (sum(d)/nnz)
     const int nparts = 304;
     double *parts = nullptr;
+    NUFFT_DEVICE_LOCK;
     NUFFT_CUDA_TRY(cudaMalloc(&parts, sizeof(double) * (nparts + 1)));
     k_sum<<<nparts, th, 0, s>>>(p->d, n, parts);
     cudaError_t e = cudaGetLastError();
@@ -373,6 +375,8 @@ extern "C" int nufft3d_normal(nufft3d_plan *p, const float *x, float *y, int nc,
 static int stage_alloc(nufft3d_plan *p, size_t in_bytes, size_t out_bytes)
 {
     HostStage &h = p->stage;
+    if (h.bytes_in >= in_bytes && h.bytes_out >= out_bytes) return NUFFT3D_SUCCESS;
+    NUFFT_DEVICE_LOCK;
     if (h.bytes_in < in_bytes) {
         if (h.in) cudaFree(h.in);
         h.in = nullptr;

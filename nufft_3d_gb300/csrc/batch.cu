@@ -48,14 +48,23 @@ struct nufft3d_batch {
     // descriptor arrays (device) and their host mirrors
     BatchFFT *fft[NFFT] = {nullptr};
     std::vector<BatchFFT> h_fft[NFFT];
-    int4 *fft_tab[NFFT] = {nullptr};
-    int fft_n[NFFT] = {0};
-    size_t fft_smem[NFFT] = {0};
+    // FFT launch groups: volumes with the same FFT length share a launch
+    struct FGroup {
+        int4 *tab;
+        int n;
+        size_t smem;
+    };
+    std::vector<FGroup> fgroups[NFFT];
     BatchInterp *gat = nullptr, *spr = nullptr;
     std::vector<BatchInterp> h_gat, h_spr;
-    int4 *itab = nullptr;
-    int in_n = 0;
-    size_t ismem = 0;
+    // interpolation launch groups: one per coil-pass width
+    struct IGroup {
+        int cb;
+        int4 *tab;
+        int n;
+        size_t smem;
+    };
+    std::vector<IGroup> igroups;
     BatchPerm *pout = nullptr, *pin = nullptr;
     std::vector<BatchPerm> h_pout, h_pin;
     int4 *ptab = nullptr;
@@ -208,6 +217,7 @@ __global__ void k_biters(const double *__restrict__ scal, int nsys, int *__restr
 template <typename T>
 static int dalloc(nufft3d_batch *b, T **p, size_t n)
 {
+    NUFFT_DEVICE_LOCK;
     if (n == 0) n = 1;
     cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
     if (e != cudaSuccess) return fail(NUFFT3D_ERR_NOMEM, std::string("batch: ") + cudaGetErrorString(e));
@@ -344,27 +354,39 @@ static int zero_grids(nufft3d_batch *b, cudaStream_t s)
     return NUFFT3D_SUCCESS;
 }
 
+static int run_fft_stage(nufft3d_batch *b, int st, int kind, cudaStream_t s)
+{
+    for (auto &g : b->fgroups[st]) NUFFT_TRY(launch_fft_batch(b->fft[st], g.tab, g.n, kind, g.smem, b->rare, s));
+    return NUFFT3D_SUCCESS;
+}
+
+static int run_interp(nufft3d_batch *b, bool gather, cudaStream_t s)
+{
+    for (auto &g : b->igroups)
+        NUFFT_TRY(launch_interp_batch(gather, g.cb, b->R, b->radial, gather ? b->gat : b->spr, g.tab, g.n, g.smem, s));
+    return NUFFT3D_SUCCESS;
+}
+
 static int run_fwd_chain(nufft3d_batch *b, cudaStream_t s)
 {
-    NUFFT_TRY(launch_fft_batch(b->fft[FX], b->fft_tab[FX], b->fft_n[FX], 0, b->fft_smem[FX], b->rare, s));
-    NUFFT_TRY(launch_fft_batch(b->fft[FY], b->fft_tab[FY], b->fft_n[FY], 1, b->fft_smem[FY], b->rare, s));
-    if (!b->is2d)
-        NUFFT_TRY(launch_fft_batch(b->fft[FZ], b->fft_tab[FZ], b->fft_n[FZ], 1, b->fft_smem[FZ], b->rare, s));
-    return launch_interp_batch(true, b->cb, b->R, b->radial, b->gat, b->itab, b->in_n, b->ismem, s);
+    NUFFT_TRY(run_fft_stage(b, FX, 0, s));
+    NUFFT_TRY(run_fft_stage(b, FY, 1, s));
+    if (!b->is2d) NUFFT_TRY(run_fft_stage(b, FZ, 1, s));
+    return run_interp(b, true, s);
 }
 
 static int run_adj_chain(nufft3d_batch *b, cudaStream_t s)
 {
     NUFFT_TRY(zero_grids(b, s));
-    NUFFT_TRY(launch_interp_batch(false, b->cb, b->R, b->radial, b->spr, b->itab, b->in_n, b->ismem, s));
-    if (!b->is2d)
-        NUFFT_TRY(launch_fft_batch(b->fft[IZ], b->fft_tab[IZ], b->fft_n[IZ], 1, b->fft_smem[IZ], b->rare, s));
-    NUFFT_TRY(launch_fft_batch(b->fft[IY], b->fft_tab[IY], b->fft_n[IY], 1, b->fft_smem[IY], b->rare, s));
-    return launch_fft_batch(b->fft[IX], b->fft_tab[IX], b->fft_n[IX], 2, b->fft_smem[IX], b->rare, s);
+    NUFFT_TRY(run_interp(b, false, s));
+    if (!b->is2d) NUFFT_TRY(run_fft_stage(b, IZ, 1, s));
+    NUFFT_TRY(run_fft_stage(b, IY, 1, s));
+    return run_fft_stage(b, IX, 2, s);
 }
 
 static void free_batch(nufft3d_batch *b)
 {
+    NUFFT_DEVICE_LOCK;
     for (void *q : b->frees) cudaFree(q);
     b->frees.clear();
     if (b->stage) cudaFreeHost(b->stage);
@@ -389,6 +411,7 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             plans[v]->geom.is2d != plans[0]->geom.is2d)
             return fail(NUFFT3D_ERR_UNSUPPORTED, "batch volumes must share ceil(J/2), the kernel type and 2-D/3-D");
     }
+    NUFFT_DEVICE_LOCK;
     int prev = -1;
     cudaGetDevice(&prev);
     const int dev = plans[0]->device;
@@ -427,31 +450,42 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
         if (needs_rare(plans[v]->fft[0]) || needs_rare(plans[v]->fft[1]) || needs_rare(plans[v]->fft[2]))
             b->rare = true;
     }
-    // descriptors and block tables
+    // descriptors and block tables; FFT launches grouped by transform length
     for (int st = 0; st < NFFT; ++st) {
         b->h_fft[st].resize(nvol);
-        std::vector<int4> tab;
-        size_t smem = 0;
+        std::vector<std::pair<int, std::vector<int4>>> groups;  // (K, table)
+        std::vector<size_t> gsmem;
         for (int v = 0; v < nvol; ++v) {
             fill_fft(b, v, &b->h_fft[st][v], st);
             const BatchFFT &d = b->h_fft[st][v];
-            const int64_t nb = fft_blocks(plans[v], d, st, nc[v]);
+            size_t gi = 0;
+            while (gi < groups.size() && groups[gi].first != d.fd.n) ++gi;
+            if (gi == groups.size()) {
+                groups.push_back({d.fd.n, {}});
+                gsmem.push_back(0);
+            }
+            std::vector<int4> &tab = groups[gi].second;
             if (st == FX || st == IX) {
                 const int nch = (nc[v] + kMaxLineCoilsHost - 1) / kMaxLineCoilsHost;
                 for (int line = 0; line < d.N23; ++line)
                     for (int c = 0; c < nch; ++c) tab.push_back(make_int4(v, line, c, 0));
-                smem = std::max(smem, line_smem(std::min(nc[v], kMaxLineCoilsHost), d.fd.n));
+                gsmem[gi] = std::max(gsmem[gi], line_smem(std::min(nc[v], kMaxLineCoilsHost), d.fd.n));
             } else {
+                const int64_t nb = fft_blocks(plans[v], d, st, nc[v]);
                 for (int64_t k = 0; k < nb; ++k) tab.push_back(make_int4(v, (int)k, 0, 0));
-                smem = std::max(smem, line_smem(d.lp.vec, d.fd.n));
+                gsmem[gi] = std::max(gsmem[gi], line_smem(d.lp.vec, d.fd.n));
             }
         }
-        b->fft_n[st] = (int)tab.size();
-        b->fft_smem[st] = smem;
-        int s2 = dalloc(b, &b->fft_tab[st], tab.size());
-        if (s2 != NUFFT3D_SUCCESS) return bail(s2);
-        if (!tab.empty() && cudaMemcpy(b->fft_tab[st], tab.data(), tab.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess)
-            return bail(fail(NUFFT3D_ERR_CUDA, "batch table upload failed"));
+        for (size_t gi = 0; gi < groups.size(); ++gi) {
+            nufft3d_batch::FGroup fg;
+            fg.n = (int)groups[gi].second.size();
+            fg.smem = gsmem[gi];
+            int s2 = dalloc(b, &fg.tab, groups[gi].second.size());
+            if (s2 != NUFFT3D_SUCCESS) return bail(s2);
+            if (fg.n && cudaMemcpy(fg.tab, groups[gi].second.data(), fg.n * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess)
+                return bail(fail(NUFFT3D_ERR_CUDA, "batch table upload failed"));
+            b->fgroups[st].push_back(fg);
+        }
     }
     {
         // interpolation: (volume, piece, first coil), heaviest pieces first
@@ -469,7 +503,11 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             if (p->n_blocks && cudaMemcpy(blk.data(), p->blocks, sizeof(int4) * p->n_blocks, cudaMemcpyDeviceToHost) != cudaSuccess)
                 return bail(fail(NUFFT3D_ERR_CUDA, "batch: reading tile pieces failed"));
             for (int64_t k = 0; k < p->n_blocks; ++k)
-                for (int c0 = 0; c0 < nc[v]; c0 += cb) ents.push_back({blk[k].z, make_int4(v, (int)k, c0, 0)});
+                for (int c0 = 0; c0 < nc[v]; c0 += cb) {
+                    int w = 1;  // this chunk's width: smallest power of two covering its coils
+                    while (w < nc[v] - c0 && w < cb) w *= 2;
+                    ents.push_back({blk[k].z, make_int4(v, (int)k, c0, w)});
+                }
             BatchInterp d;
             std::memset(&d, 0, sizeof(d));
             d.samples = p->samples;
@@ -484,16 +522,23 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             maxcand = std::max(maxcand, p->n_cand);
         }
         std::stable_sort(ents.begin(), ents.end(), [](const E &a, const E &c) { return a.count > c.count; });
-        std::vector<int4> tab;
-        for (auto &e : ents) tab.push_back(e.e);
-        b->in_n = (int)tab.size();
-        const size_t plane = smem_plane_bytes(b->R, cb);
-        const size_t iplane = (size_t)(((plane / (cb * sizeof(float2)) + 29) / 32) * 32 + 2) * cb * 2 * sizeof(int);
-        b->ismem = std::max(plane, iplane) + cand_smem_bytes(maxcand);
-        int s2 = dalloc(b, &b->itab, tab.size());
-        if (s2 != NUFFT3D_SUCCESS) return bail(s2);
-        if (!tab.empty() && cudaMemcpy(b->itab, tab.data(), tab.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess)
-            return bail(fail(NUFFT3D_ERR_CUDA, "batch table upload failed"));
+        for (int w = cb; w >= 1; w /= 2) {
+            std::vector<int4> tab;
+            for (auto &e : ents)
+                if (e.e.w == w) tab.push_back(make_int4(e.e.x, e.e.y, e.e.z, 0));
+            if (tab.empty()) continue;
+            nufft3d_batch::IGroup ig;
+            ig.cb = w;
+            ig.n = (int)tab.size();
+            const size_t plane = smem_plane_bytes(b->R, w);
+            const size_t iplane = (size_t)(((plane / (w * sizeof(float2)) + 29) / 32) * 32 + 2) * w * 2 * sizeof(int);
+            ig.smem = std::max(plane, iplane) + cand_smem_bytes(maxcand);
+            int s2 = dalloc(b, &ig.tab, tab.size());
+            if (s2 != NUFFT3D_SUCCESS) return bail(s2);
+            if (cudaMemcpy(ig.tab, tab.data(), tab.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess)
+                return bail(fail(NUFFT3D_ERR_CUDA, "batch table upload failed"));
+            b->igroups.push_back(ig);
+        }
     }
     {
         std::vector<int4> tab;
@@ -550,7 +595,13 @@ extern "C" int nufft3d_batch_destroy(nufft3d_batch *b)
 {
     clear_error();
     if (!b) return NUFFT3D_SUCCESS;
-    cudaDeviceSynchronize();
+    {
+        NUFFT_DEVICE_LOCK;
+        cudaStreamSynchronize(b->own);
+        for (int v = 0; v < b->nvol; ++v)
+            if (b->plans[v]->own_stream) cudaStreamSynchronize(b->plans[v]->own_stream);
+        cudaDeviceSynchronize();
+    }
     free_batch(b);
     delete b;
     return NUFFT3D_SUCCESS;
@@ -665,6 +716,7 @@ extern "C" int nufft3d_batch_inverse(nufft3d_batch *b, const float *const *raw, 
         NUFFT_TRY(upload(b, s));
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
+        NUFFT_DEVICE_LOCK;
         NUFFT_CUDA_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
         int st = run_fwd_chain(b, s);
         if (st == NUFFT3D_SUCCESS) st = run_adj_chain(b, s);
@@ -697,6 +749,7 @@ extern "C" int nufft3d_batch_inverse(nufft3d_batch *b, const float *const *raw, 
     }
     if (iters_host) {
         int *di = nullptr;
+        NUFFT_DEVICE_LOCK;
         NUFFT_CUDA_TRY(cudaMalloc(&di, sizeof(int) * b->nsys));
         k_biters<<<nsb, tb, 0, s>>>(b->scal, b->nsys, di);
         cudaMemcpyAsync(iters_host, di, sizeof(int) * b->nsys, cudaMemcpyDeviceToHost, s);

@@ -4,12 +4,22 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
 #include "../../include/nufft3d.h"
 
 namespace nufft3d {
+
+// ------------------------------------------------------ device lock
+// CUDA graph capture on one thread is invalidated when another thread makes a
+// device-wide synchronising call (cudaFree, cudaDeviceSynchronize).  Every
+// allocation, free and device-wide synchronisation in the library, and every
+// capture, holds this lock, so plans can be built, freed and used from several
+// threads at once (the serving loop does).
+std::recursive_mutex &device_lock();
+#define NUFFT_DEVICE_LOCK std::lock_guard<std::recursive_mutex> nufft_dlk_(::nufft3d::device_lock())
 
 // ---------------------------------------------------------------- errors
 void set_error(const std::string &msg);

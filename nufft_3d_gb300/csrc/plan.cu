@@ -25,6 +25,12 @@
 
 namespace nufft3d {
 
+std::recursive_mutex &device_lock()
+{
+    static std::recursive_mutex mu;
+    return mu;
+}
+
 // ------------------------------------------------------------- errors
 static thread_local std::string g_last_error;
 
@@ -320,6 +326,7 @@ int configure_kernels()
 
 TableOwner::~TableOwner()
 {
+    NUFFT_DEVICE_LOCK;
     int prev = -1;
     if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
     if (prev != device) cudaSetDevice(device);
@@ -341,6 +348,7 @@ static void adopt_tables(nufft3d_plan *p)
 // Free what the plan owns by itself; tables go with the last sharer.
 static void free_plan_memory(nufft3d_plan *p)
 {
+    NUFFT_DEVICE_LOCK;
     auto F = [](void *ptr) {
         if (ptr) cudaFree(ptr);
     };
@@ -386,6 +394,7 @@ struct DeviceGuard {
 template <typename T>
 static int dmalloc(T **ptr, size_t count, int64_t *acc)
 {
+    NUFFT_DEVICE_LOCK;
     if (count == 0) count = 1;
     cudaError_t e = cudaMalloc((void **)ptr, count * sizeof(T));
     if (e != cudaSuccess) {
@@ -407,6 +416,7 @@ static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts
         std::vector<void *> ptrs;
         ~Tmp()
         {
+            NUFFT_DEVICE_LOCK;
             for (void *q : ptrs) cudaFree(q);
         }
     } tmp;
@@ -448,7 +458,7 @@ static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts
     NUFFT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(nullptr, tb, keys, keys_sorted, vals, p->perm,
                                                    (int)M, 0, end_bit, s));
     void *tstore = nullptr;
-    NUFFT_CUDA_TRY(cudaMalloc(&tstore, tb ? tb : 1));
+    NUFFT_TRY(dmalloc((char **)&tstore, tb ? tb : 1, nullptr));
     tmp.ptrs.push_back(tstore);
     NUFFT_CUDA_TRY(cub::DeviceRadixSort::SortPairs(tstore, tb, keys, keys_sorted, vals, p->perm,
                                                    (int)M, 0, end_bit, s));
@@ -497,7 +507,7 @@ static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts
         k_records<<<(unsigned)((nnz + th - 1) / th), th, 0, s>>>(om_dev, p->perm, nnz, kp, p->samples, p->inv);
         NUFFT_CUDA_TRY(cudaGetLastError());
         unsigned long long *tot = nullptr;
-        NUFFT_CUDA_TRY(cudaMalloc(&tot, sizeof(unsigned long long)));
+        NUFFT_TRY(dmalloc(&tot, 1, nullptr));
         tmp.ptrs.push_back(tot);
         NUFFT_CUDA_TRY(cudaMemsetAsync(tot, 0, sizeof(unsigned long long), s));
         const unsigned nbs = (unsigned)((nnz + th - 1) / th);
@@ -722,6 +732,7 @@ extern "C" int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **out)
     clear_error();
     if (!src || !out) return fail(NUFFT3D_ERR_ARG, "NULL argument");
     *out = nullptr;
+    NUFFT_DEVICE_LOCK;
     DeviceGuard guard(src->device);
     nufft3d_plan *p = new nufft3d_plan();
     p->device = src->device;
@@ -781,8 +792,9 @@ extern "C" int nufft3d_plan_destroy(nufft3d_plan *p)
     clear_error();
     if (!p) return NUFFT3D_SUCCESS;
     {
+        NUFFT_DEVICE_LOCK;
         DeviceGuard guard(p->device);
-        cudaDeviceSynchronize();
+        if (p->own_stream) cudaStreamSynchronize(p->own_stream);
         free_plan_memory(p);
     }
     delete p;

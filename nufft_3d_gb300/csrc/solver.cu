@@ -317,7 +317,10 @@ int prepare_weights(nufft3d_plan *p, const float *W_orig, const float **wsorted,
         *wsorted = p->d;
         return NUFFT3D_SUCCESS;
     }
-    if (!p->wbuf) NUFFT_CUDA_TRY(cudaMalloc(&p->wbuf, sizeof(float) * (p->nnz > 0 ? p->nnz : 1)));
+    if (!p->wbuf) {
+        NUFFT_DEVICE_LOCK;
+        NUFFT_CUDA_TRY(cudaMalloc(&p->wbuf, sizeof(float) * (p->nnz > 0 ? p->nnz : 1)));
+    }
     if (p->nnz > 0) {
         k_weights<<<(unsigned)((p->nnz + 255) / 256), 256, 0, s>>>(W_orig, p->perm, p->d, p->nnz, p->wbuf);
         NUFFT_CUDA_TRY(cudaGetLastError());
@@ -331,6 +334,7 @@ int ensure_solver(nufft3d_plan *p, int nc)
     SolverWork &w = p->solver;
     const size_t nimg = (size_t)p->N[0] * p->N[1] * p->N[2];
     if (w.nc >= nc && w.nimg == nimg) return NUFFT3D_SUCCESS;
+    NUFFT_DEVICE_LOCK;
     float2 **vecs[] = {&w.r, &w.p, &w.q, &w.v, &w.vprev, &w.w1, &w.w2};
     for (auto pp : vecs)
         if (*pp) {
@@ -429,17 +433,22 @@ int run_inverse(nufft3d_plan *p, const float2 *raw, float2 *x, int nc, int maxit
         // capture one iteration and replay it maxit times
         cudaGraph_t graph = nullptr;
         cudaGraphExec_t exec = nullptr;
-        NUFFT_CUDA_TRY(cudaStreamBeginCapture(own, cudaStreamCaptureModeThreadLocal));
-        int st = solver == NUFFT3D_SOLVER_CG ? cg_iteration(p, x, nc, damp, ws, own)
+        int st;
+        cudaError_t ce;
+        {
+            NUFFT_DEVICE_LOCK;
+            NUFFT_CUDA_TRY(cudaStreamBeginCapture(own, cudaStreamCaptureModeThreadLocal));
+            st = solver == NUFFT3D_SOLVER_CG ? cg_iteration(p, x, nc, damp, ws, own)
                                              : minres_iteration(p, x, nc, damp, ws, own);
-        cudaError_t ce = cudaStreamEndCapture(own, &graph);
-        if (st != NUFFT3D_SUCCESS) {
+            ce = cudaStreamEndCapture(own, &graph);
+            if (st == NUFFT3D_SUCCESS && ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
             if (graph) cudaGraphDestroy(graph);
+        }
+        if (st != NUFFT3D_SUCCESS) {
+            if (exec) cudaGraphExecDestroy(exec);
             return st;
         }
         if (ce != cudaSuccess) return fail(NUFFT3D_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
-        ce = cudaGraphInstantiate(&exec, graph, 0);
-        cudaGraphDestroy(graph);
         if (ce != cudaSuccess) return fail(NUFFT3D_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
         for (int it = 0; it < maxit && ce == cudaSuccess; ++it) ce = cudaGraphLaunch(exec, own);
         cudaGraphExecDestroy(exec);
@@ -513,6 +522,8 @@ extern "C" int nufft3d_inverse_host(nufft3d_plan *p, const float *raw, float *x,
     const size_t bW = W ? (size_t)p->M * sizeof(float) : 0;
     const size_t bx = (size_t)p->N[0] * p->N[1] * p->N[2] * nc * sizeof(float2);
     HostStage &h = p->stage;
+    if (h.bytes_in < braw + bW + 256 || h.bytes_out < bx) {
+        NUFFT_DEVICE_LOCK;
     if (h.bytes_in < braw + bW + 256) {
         if (h.in) cudaFree(h.in);
         h.in = nullptr;
@@ -526,6 +537,7 @@ extern "C" int nufft3d_inverse_host(nufft3d_plan *p, const float *raw, float *x,
         h.bytes_out = 0;
         NUFFT_CUDA_TRY(cudaMalloc(&h.out, bx));
         h.bytes_out = bx;
+    }
     }
     cudaStream_t s = p->own_stream;
     char *base = (char *)h.in;

@@ -271,16 +271,18 @@ class ReconServer:
 def run_served(requests, slots=4, hbm_budget=None, device=0, max_batch_coils=16, t0=None):
     """Feed requests at their arrival times; returns (requests, wall seconds)."""
     srv = ReconServer(slots=slots, hbm_budget=hbm_budget, device=device, max_batch_coils=max_batch_coils)
-    futs = []
-    start = time.perf_counter() if t0 is None else t0
-    for r in sorted(requests, key=lambda r: r.arrival):
-        delay = start + r.arrival - time.perf_counter()
-        if delay > 0:
-            time.sleep(delay)
-        futs.append(srv.submit(r))
-    done = [f.result() for f in futs]
-    wall = time.perf_counter() - start
-    srv.close()
+    try:
+        futs = []
+        start = time.perf_counter() if t0 is None else t0
+        for r in sorted(requests, key=lambda r: r.arrival):
+            delay = start + r.arrival - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            futs.append(srv.submit(r))
+        done = [f.result() for f in futs]
+        wall = time.perf_counter() - start
+    finally:
+        srv.close()
     for r in done:
         r.t_done -= start
         r.t_start -= start
