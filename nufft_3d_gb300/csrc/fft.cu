@@ -202,6 +202,176 @@ __device__ __forceinline__ int slot_of(int n, int N, int K)
     return s < 0 ? s + K : s;
 }
 
+// ------------------------------------------------ four-step line passes
+// In-register DFTs of 12, 16, 20 and 24 points built from the radix 3/4/5/8
+// butterflies (n = B*a + b, k = ka + A*kb), with the W_AB twiddles read from
+// constant memory at compile-time indices (tables filled once per device from
+// FP64 values).
+__constant__ float2 c_w12[12];
+__constant__ float2 c_w16[16];
+__constant__ float2 c_w20[20];
+__constant__ float2 c_w24[24];
+
+template <int N>
+__device__ __forceinline__ float2 wconst(int j);
+template <> __device__ __forceinline__ float2 wconst<12>(int j) { return c_w12[j]; }
+template <> __device__ __forceinline__ float2 wconst<16>(int j) { return c_w16[j]; }
+template <> __device__ __forceinline__ float2 wconst<20>(int j) { return c_w20[j]; }
+template <> __device__ __forceinline__ float2 wconst<24>(int j) { return c_w24[j]; }
+
+template <int A, int B>
+__device__ __forceinline__ void dft_comp(float2 (&u)[A * B])
+{
+    float2 t[A * B];
+#pragma unroll
+    for (int b = 0; b < B; ++b) {
+        float2 v[A];
+#pragma unroll
+        for (int a = 0; a < A; ++a) v[a] = u[B * a + b];
+        dft<A>(v, nullptr, 0);
+#pragma unroll
+        for (int ka = 0; ka < A; ++ka) {
+            float2 x = v[ka];
+            if (b != 0 && ka != 0) x = cmul(x, wconst<A * B>((b * ka) % (A * B)));
+            t[b * A + ka] = x;
+        }
+    }
+#pragma unroll
+    for (int ka = 0; ka < A; ++ka) {
+        float2 v[B];
+#pragma unroll
+        for (int b = 0; b < B; ++b) v[b] = t[b * A + ka];
+        dft<B>(v, nullptr, 0);
+#pragma unroll
+        for (int kb = 0; kb < B; ++kb) u[ka + A * kb] = v[kb];
+    }
+}
+
+template <int R>
+__device__ __forceinline__ void dft_reg(float2 (&u)[R]);
+template <> __device__ __forceinline__ void dft_reg<8>(float2 (&u)[8]) { dft<8>(u, nullptr, 0); }
+template <> __device__ __forceinline__ void dft_reg<12>(float2 (&u)[12]) { dft_comp<3, 4>(u); }
+template <> __device__ __forceinline__ void dft_reg<16>(float2 (&u)[16]) { dft_comp<4, 4>(u); }
+template <> __device__ __forceinline__ void dft_reg<20>(float2 (&u)[20]) { dft_comp<4, 5>(u); }
+template <> __device__ __forceinline__ void dft_reg<24>(float2 (&u)[24]) { dft_comp<3, 8>(u); }
+
+// Strided pass (y or z) for K = R1 * 16 over lp.vec = 16 contiguous lines:
+// X[k1 + R1 k2] = sum_n2 W16^(n2 k2) W_K^(n2 k1) sum_n1 x[16 n1 + n2] W_R1^(n1 k1).
+// Pass 1 (lanes over lines, n2 outer): DFT_R1 in registers, twiddle, store to
+// shared memory; pass 2: DFT_16 in registers, store.  Lane -> line mapping
+// keeps global accesses coalesced (a line is one complex of a contiguous row)
+// and the row stride K+1 keeps shared-memory accesses conflict-free.
+template <int R1>
+__global__ void __launch_bounds__(384)
+k_line4(const float2 *__restrict__ in, float2 *__restrict__ out, LinePass lp, const float2 *__restrict__ twg,
+        int inv)
+{
+    constexpr int R2 = 16, K = R1 * R2, L = 16, LS = K + 1;
+    extern __shared__ float2 sm[];
+    float2 *Y = sm;
+    float2 *tw = sm + L * LS;
+    for (int t = threadIdx.x; t < K; t += blockDim.x) tw[t] = twg[t];
+    const int outer = blockIdx.x / lp.nchunks;
+    const int chunk = blockIdx.x - outer * lp.nchunks;
+    const float2 *ib = in + outer * lp.in_outer_stride + (int64_t)chunk * L;
+    float2 *ob = out + outer * lp.out_outer_stride + (int64_t)chunk * L;
+    const float sg = inv ? -1.f : 1.f;
+    // slot map (n - N/2) mod K: slots [0, N - N/2) hold n = slot + N/2,
+    // slots [K - N/2, K) hold n = slot - (K - N/2), the rest are zero padding
+    const int Nh = lp.Nimg / 2, Nt = lp.Nimg - Nh;
+    __syncthreads();
+    for (int it = threadIdx.x; it < L * R2; it += blockDim.x) {
+        const int line = it % L, n2 = it / L;
+        float2 u[R1];
+#pragma unroll
+        for (int n1 = 0; n1 < R1; ++n1) {
+            const int pos = n2 + R2 * n1;
+            int src = pos;
+            if (lp.pad_in) src = pos < Nt ? pos + Nh : (pos >= K - Nh ? pos - (K - Nh) : -1);
+            float2 v = make_float2(0.f, 0.f);
+            if (src >= 0) {
+                v = ib[(int64_t)src * lp.in_axis_stride + line];
+                v.y *= sg;
+            }
+            u[n1] = v;
+        }
+        dft_reg<R1>(u);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; ++k1) {
+            float2 x = u[k1];
+            if (k1) x = cmul(x, tw[n2 * k1]);
+            Y[line * LS + k1 * R2 + n2] = x;
+        }
+    }
+    __syncthreads();
+    for (int it = threadIdx.x; it < L * R1; it += blockDim.x) {
+        const int line = it % L, k1 = it / L;
+        float2 u[R2];
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) u[n2] = Y[line * LS + k1 * R2 + n2];
+        dft_reg<R2>(u);
+#pragma unroll
+        for (int k2 = 0; k2 < R2; ++k2) {
+            const int k = k1 + R1 * k2;
+            int dst = k;
+            if (lp.crop_out) dst = k < Nt ? k + Nh : (k >= K - Nh ? k - (K - Nh) : -1);
+            if (dst >= 0) {
+                const float2 r = u[k2];
+                ob[(int64_t)dst * lp.out_axis_stride + line] = make_float2(r.x, sg * r.y);
+            }
+        }
+    }
+}
+
+static int four_step_r1(int K, int vec)
+{
+    if (vec != 16) return 0;
+    switch (K) {
+    case 128: return 8;
+    case 192: return 12;
+    case 256: return 16;
+    case 320: return 20;
+    case 384: return 24;
+    default: return 0;
+    }
+}
+
+static size_t line4_smem(int K) { return (size_t)(16 * (K + 1) + K) * sizeof(float2); }
+
+static int launch_line4(int r1, const float2 *in, float2 *out, const LinePass &lp, const FFTDesc &fd, int inv,
+                        int64_t nblk, cudaStream_t s)
+{
+    const int K = fd.n;
+    const int threads = 16 * (r1 > 16 ? r1 : 16);
+    const size_t smem = line4_smem(K);
+    switch (r1) {
+    case 8: k_line4<8><<<(unsigned)nblk, threads, smem, s>>>(in, out, lp, fd.tw, inv); break;
+    case 12: k_line4<12><<<(unsigned)nblk, threads, smem, s>>>(in, out, lp, fd.tw, inv); break;
+    case 16: k_line4<16><<<(unsigned)nblk, threads, smem, s>>>(in, out, lp, fd.tw, inv); break;
+    case 20: k_line4<20><<<(unsigned)nblk, threads, smem, s>>>(in, out, lp, fd.tw, inv); break;
+    default: k_line4<24><<<(unsigned)nblk, threads, smem, s>>>(in, out, lp, fd.tw, inv); break;
+    }
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
+int configure_fft_constants()
+{
+    auto fill = [](const void *sym, int n) {
+        std::vector<float2> w(n);
+        for (int j = 0; j < n; ++j) {
+            const double a = -2.0 * M_PI * j / n;
+            w[j] = make_float2((float)std::cos(a), (float)std::sin(a));
+        }
+        return cudaMemcpyToSymbol(sym, w.data(), n * sizeof(float2));
+    };
+    NUFFT_CUDA_TRY(fill(c_w12, 12));
+    NUFFT_CUDA_TRY(fill(c_w16, 16));
+    NUFFT_CUDA_TRY(fill(c_w20, 20));
+    NUFFT_CUDA_TRY(fill(c_w24, 24));
+    return NUFFT3D_SUCCESS;
+}
+
 // ------------------------------------------------------------- kernels
 constexpr int kFftThreads = 256;
 constexpr int kMaxLineCoils = 16;
@@ -393,6 +563,8 @@ static int launch_line(const float2 *in, float2 *out, int n_outer, int64_t rowle
                                       in_outer, out_outer, &nblk);
     if (nblk <= 0) return NUFFT3D_SUCCESS;
     if (nblk > 0x7fffffff) return fail(NUFFT3D_ERR_SIZE, "FFT pass grid too large");
+    const int r1 = four_step_r1(fd.n, lp.vec);
+    if (r1) return launch_line4(r1, in, out, lp, fd, inv, nblk, s);
     if (needs_rare(fd))
         k_line<true><<<(unsigned)nblk, kFftThreads, line_smem(lp.vec, fd.n), s>>>(in, out, lp, fd, inv);
     else
@@ -509,7 +681,12 @@ int configure_fft_kernels()
     NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
     NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fft_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
     NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fft_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    return NUFFT3D_SUCCESS;
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line4<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line4<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line4<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line4<20>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line4<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    return configure_fft_constants();
 }
 
 } // namespace nufft3d

@@ -184,6 +184,28 @@ __device__ __forceinline__ int eval_chunk(int base, const SampleGeo &sg, const C
 
 // Gather: tile staged coil-major ([CB][P^3] complex) -> ks.  kGroup lanes per
 // sample walk the candidate list; partial sums are reduced across the group.
+// acc[c] += w * tile(c, off): coil pairs come from one 16-byte load of a pair
+// plane (conflict-free: a quarter-warp is one sample's 8 neighbouring taps).
+template <int CB, int PV>
+__device__ __forceinline__ void accumulate(float2 (&acc)[CB], const float2 *tile, int off, float w)
+{
+    if (CB >= 2) {
+        const float4 *t4 = reinterpret_cast<const float4 *>(tile);
+#pragma unroll
+        for (int q = 0; q < CB / 2; ++q) {
+            const float4 v = t4[(size_t)q * PV + off];
+            acc[2 * q].x = fmaf(w, v.x, acc[2 * q].x);
+            acc[2 * q].y = fmaf(w, v.y, acc[2 * q].y);
+            acc[2 * q + 1].x = fmaf(w, v.z, acc[2 * q + 1].x);
+            acc[2 * q + 1].y = fmaf(w, v.w, acc[2 * q + 1].y);
+        }
+    } else {
+        const float2 v = tile[off];
+        acc[0].x = fmaf(w, v.x, acc[0].x);
+        acc[0].y = fmaf(w, v.y, acc[0].y);
+    }
+}
+
 template <int CB, bool RADIAL, int R>
 __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
                                             const float4 *__restrict__ samples, const int4 bi, const Geom &g,
@@ -204,7 +226,8 @@ __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2
     const int cb = min(CB, nc - c0);
     // stage the padded tile with asynchronous copies (no register round trip)
     for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int c, size_t gidx) {
-        float2 *dst = &tile[c * pv + pt];
+        // coil pairs in float4 planes: coil c of point pt at float2 (c/2)*2*pv + 2*pt + (c&1)
+        float2 *dst = CB >= 2 ? &tile[(size_t)(c >> 1) * 2 * pv + 2 * pt + (c & 1)] : &tile[pt];
         if (c < cb) {
             const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
             asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(&G[gidx * nc + c0 + c]) : "memory");
@@ -236,22 +259,8 @@ __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2
             int off0, off1;
             const bool h0 = ci0 < cd.n && tap<RADIAL>(ci0, sg, cs, kb, w0, off0);
             const bool h1 = ci1 < cd.n && tap<RADIAL>(ci1, sg, cs, kb, w1, off1);
-            if (h0) {
-#pragma unroll
-                for (int c = 0; c < CB; ++c) {
-                    const float2 v = tile[c * pv + off0];
-                    acc[c].x = fmaf(w0, v.x, acc[c].x);
-                    acc[c].y = fmaf(w0, v.y, acc[c].y);
-                }
-            }
-            if (h1) {
-#pragma unroll
-                for (int c = 0; c < CB; ++c) {
-                    const float2 v = tile[c * pv + off1];
-                    acc[c].x = fmaf(w1, v.x, acc[c].x);
-                    acc[c].y = fmaf(w1, v.y, acc[c].y);
-                }
-            }
+            if (h0) accumulate<CB, pv>(acc, tile, off0, w0);
+            if (h1) accumulate<CB, pv>(acc, tile, off1, w1);
         }
 #pragma unroll
         for (int c = 0; c < CB; ++c) {

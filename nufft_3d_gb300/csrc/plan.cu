@@ -318,6 +318,7 @@ int configure_kernels()
     NUFFT_CUDA_TRY(cudaGetDevice(&dev));
     std::lock_guard<std::mutex> lk(mu);
     if (dev < 32 && (done_mask & (1 << dev))) return NUFFT3D_SUCCESS;
+    NUFFT_DEVICE_LOCK; // constant-memory uploads must not overlap a stream capture
     NUFFT_TRY(configure_fft_kernels());
     NUFFT_TRY(configure_interp_kernels());
     if (dev < 32) done_mask |= 1 << dev;

@@ -195,3 +195,20 @@ def test_minres_tolerance_stop(cuda):
     assert all(abs(a - b) <= 1 for a, b in zip(its, ref.last_iters)), (its, ref.last_iters)
     assert max(its) < 200
     assert rel(im, imr) < 1e-3
+
+
+@pytest.mark.parametrize("N,nc", [((64, 96, 160), 2), ((128, 192, 32), 1), ((160, 64, 128), 3)])
+def test_fft_lengths_non_cubic(cuda, N, nc):
+    """Oversampled lengths K = 128, 192, 256, 320, 384 on every axis and pass
+    (register four-step and shared-memory Stockham line FFTs), non-cubic N."""
+    torch = cuda
+    rng = np.random.default_rng(sum(N) + nc)
+    M = 3000
+    om = np.vstack([rng.uniform(-n / 2, n / 2 - 1, M) for n in N])
+    obj = nufft_3d(om, np.array(N), "J", 6, density_iters=0)
+    ref = NufftRef(om, np.array(N), J=6, density_iters=0)
+    assert list(obj.K) == [2 * n for n in N]
+    x = rng.standard_normal(tuple(N) + (nc,)) + 1j * rng.standard_normal(tuple(N) + (nc,))
+    y = rng.standard_normal((M, nc)) + 1j * rng.standard_normal((M, nc))
+    assert rel(k_from_dev(obj.fNUFT(img_to_dev(torch, x))), ref.fNUFT(x)) < TOL_OP
+    assert rel(img_from_dev(obj.aNUFT(k_to_dev(torch, y))), ref.aNUFT(y)) < TOL_OP
