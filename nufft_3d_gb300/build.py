@@ -15,6 +15,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libnufft3d.so")
+INCLUDE = os.path.join(os.path.dirname(HERE), "include")
+HARNESS_SRC = os.path.join(HERE, "c_harness", "nufft3d_harness.c")
+HARNESS = os.path.join(HERE, "c_harness", "nufft3d_harness")
 SOURCES = ["plan.cu", "api.cu", "fft.cu", "interp.cu", "solver.cu", "noalloc.cu", "batch.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
@@ -57,6 +60,18 @@ def build(verbose_ptxas=False, jobs=None):
     return LIB
 
 
+def build_harness(out=HARNESS):
+    """Compiles the plain C host (nufft3d_harness.c) against libnufft3d.so."""
+    cc = os.environ.get("CC") or shutil.which("gcc") or "cc"
+    cmd = [cc, "-std=c99", "-O2", "-Wall", "-Wextra", "-D_DEFAULT_SOURCE", "-I", INCLUDE, HARNESS_SRC, "-o", out,
+           "-L", HERE, "-lnufft3d", "-lm", "-Wl,-rpath," + HERE]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("harness build failed:\n%s\n%s" % (r.stdout, r.stderr))
+    return out
+
+
 if __name__ == "__main__":
     build(verbose_ptxas="-v" in sys.argv)
+    build_harness()
     print(LIB)
