@@ -185,7 +185,8 @@ __device__ __forceinline__ int eval_chunk(int base, const SampleGeo &sg, const C
 // Gather: tile staged coil-major ([CB][P^3] complex) -> ks.  kGroup lanes per
 // sample walk the candidate list; partial sums are reduced across the group.
 // acc[c] += w * tile(c, off): coil pairs come from one 16-byte load of a pair
-// plane (conflict-free: a quarter-warp is one sample's 8 neighbouring taps).
+// plane; a quarter-warp is one sample's chunk of 8 candidates, whose tile
+// words the plan-time candidate order spreads over distinct bank groups.
 template <int CB, int PV>
 __device__ __forceinline__ void accumulate(float2 (&acc)[CB], const float2 *tile, int off, float w)
 {
@@ -296,8 +297,10 @@ k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
 // so that every partial sum stays below 2^30 and every product w*y*2^F below
 // 2^22; products are rounded to integers exactly by the 1.5*2^23 addition.
 // Layout [CB][2][P^3] int32 (split real/imaginary planes, so a warp's
-// scattered taps spread over all banks).  Lanes of a group touch distinct
-// taps; the groups of a warp start on different candidate shells.  The tile
+// scattered taps spread over all banks).  A warp takes one sample: its hits
+// are compacted into a queue and each quarter-warp adds one coil pair of 8
+// queued taps per instruction (the candidate order keeps those 8 offsets in
+// distinct bank groups where it can).  The tile
 // is then added to the grid with vector atomics (neighbouring tiles' halos
 // overlap).
 __device__ __forceinline__ float block_max(float v, float *red)

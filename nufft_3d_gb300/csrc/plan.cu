@@ -15,12 +15,15 @@
 #include <complex>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include <cub/device/device_radix_sort.cuh>
 
+#include "bank_order.h"
 #include "internal.h"
 
 namespace nufft3d {
@@ -150,8 +153,9 @@ static std::vector<double> deap_host(const int N[3], const int K[3], double J, d
 
 // Candidate taps for the octant f in [0, 1/2]^3 (samples are reflected onto
 // it): offsets d' in [-R, R]^3 whose smallest possible distance over that
-// octant is inside the support, ordered so that offsets inside the support
-// for every f come first.  A relative slack of 1e-5 keeps every tap that the
+// octant is inside the support, ordered near to far (offsets inside the
+// support for every f first; bank_order then re-partitions nearby chunks of 8
+// for shared-memory banks).  A relative slack of 1e-5 keeps every tap that the
 // single-precision test in the kernels can accept.
 static std::vector<int> make_candidates(int R, int radial, int is2d, double J)
 {
@@ -181,21 +185,24 @@ static std::vector<int> make_candidates(int R, int radial, int is2d, double J)
     std::stable_sort(v.begin(), v.end(), [](const C &a, const C &b) {
         return a.key != b.key ? a.key < b.key : a.key2 < b.key2;
     });
-    // within each chunk of 8 (one iteration of a lane group) order row-major so
-    // the group's lanes touch neighbouring words of the tile (fewer conflicts)
-    for (size_t i = 0; i < v.size(); i += 8) {
-        const size_t e = std::min(v.size(), i + 8);
-        std::sort(v.begin() + i, v.begin() + e, [](const C &a, const C &b) {
-            const int za = a.code >> 8, zb = b.code >> 8;
-            const int ya = (a.code >> 4) & 15, yb = (b.code >> 4) & 15;
-            if (za != zb) return za < zb;
-            if (ya != yb) return ya < yb;
-            return (a.code & 15) < (b.code & 15);
-        });
-    }
     std::vector<int> out;
     for (auto &c : v) out.push_back(c.code);
     return out;
+}
+
+// make_candidates + bank_order, cached per geometry (the search takes ~0.1 s)
+static std::vector<int> ordered_candidates(int R, int radial, int is2d, double J, int Px, int PxPy)
+{
+    static std::mutex mu;
+    static std::map<std::tuple<int, int, int, double, int, int>, std::vector<int>> cache;
+    const auto key = std::make_tuple(R, radial, is2d, J, Px, PxPy);
+    std::lock_guard<std::mutex> lk(mu);
+    auto it = cache.find(key);
+    if (it != cache.end()) return it->second;
+    std::vector<int> c = make_candidates(R, radial, is2d, J);
+    bank_order(c, Px, PxPy, J, radial, is2d);
+    cache.emplace(key, c);
+    return c;
 }
 
 // ------------------------------------------------------ device kernels
@@ -527,7 +534,7 @@ static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts
     }
 
     {
-        std::vector<int> cand = make_candidates(g.R, g.radial, g.is2d, p->J);
+        std::vector<int> cand = ordered_candidates(g.R, g.radial, g.is2d, p->J, g.P[0], g.P[0] * g.P[1]);
         if (cand.size() > 512) return fail(NUFFT3D_ERR_UNSUPPORTED, "too many candidate taps");
         p->n_cand = (int)cand.size();
         NUFFT_TRY(dmalloc(&p->cand, cand.size(), &p->table_bytes));
