@@ -46,6 +46,9 @@ int fail(int code, const std::string &msg);
 // with the Numerical Recipes I0 polynomial (kernel.m:14-30).  The large-
 // argument branch is rearranged as exp(ax - alpha) * rsqrt(ax) * poly *
 // (exp(alpha)/I0(alpha)) so no intermediate leaves single-precision range.
+// Degree of the plan-time polynomial fit of the Kaiser-Bessel kernel.
+constexpr int kKBDeg = 14;
+
 struct KBParams {
     float alpha;        // KB alpha
     float inv_half2;    // 1/(J/2)^2
@@ -53,6 +56,8 @@ struct KBParams {
     float inv_i0a;      // 1/I0(alpha)
     float exp_over_i0a; // exp(alpha)/I0(alpha)
     float half2;        // (J/2)^2: tap kept iff dist2 <= half2 (4*dist2 <= J^2)
+    int poly;           // 1: use the polynomial c below (fitted at plan time)
+    float c[kKBDeg + 1]; // kernel(t) ~ sum_k c[k] t^k, t = 1 - dist2/(J/2)^2
 };
 
 // exp(x) for x <= 0 by Cody-Waite range reduction: x*log2(e) = hi + lo with
@@ -73,6 +78,14 @@ __device__ __forceinline__ float kb_weight(float dist2, const KBParams &p)
 {
     // (J/2)^2 - dist2 is exact for dist2 in [(J/2)^2/2, (J/2)^2] (Sterbenz)
     const float t = fmaxf((p.half2 - dist2) * p.inv_half2, 0.0f);
+    if (p.poly) {
+        // branch-free: a degree-14 polynomial in t interpolating the same
+        // kernel at Chebyshev nodes (max error checked at plan time)
+        float s = p.c[kKBDeg];
+#pragma unroll
+        for (int k = kKBDeg - 1; k >= 0; --k) s = fmaf(s, t, p.c[k]);
+        return s;
+    }
     const float y = p.a2_over * t; // (ax/3.75)^2
     if (y < 1.0f) {
         float s = fmaf(y, 0.45813e-2f, 0.360768e-1f);

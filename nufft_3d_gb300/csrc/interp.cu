@@ -52,11 +52,26 @@ struct Cand {
 
 // Per-block candidate tables in shared memory: offsets as floats for the
 // distance test and the tile offset of each candidate in each of the 8 sign
-// octants.
+// octants, octant-major so that lanes reading consecutive candidates of one
+// octant hit consecutive banks; the octant stride is 8 mod 32 so that lane
+// groups reading the same candidates in different octants shift banks.
 struct CandSmem {
-    float4 *f;  // [n] (dx', dy', dz', 0)
-    int *off;   // [n][8]
+    float4 *f;   // [n] (dx', dy', dz', 0)
+    int *off;    // [8][stride]
+    int stride;
 };
+
+__host__ __device__ __forceinline__ int cand_stride(int n) { return n + ((8 - n % 32) + 32) % 32; }
+
+// Candidate tables at the start of the dynamic shared memory; returns the
+// first free 16-byte word after them.
+__device__ __forceinline__ float4 *carve_cand(const Cand &cd, CandSmem &cs, float4 *smem4)
+{
+    cs.stride = cand_stride(cd.n);
+    cs.f = smem4;
+    cs.off = reinterpret_cast<int *>(smem4 + cd.n);
+    return smem4 + cd.n + 2 * cs.stride;
+}
 
 __device__ __forceinline__ void build_cand(const Cand &cd, CandSmem cs, int Px, int PxPy)
 {
@@ -67,12 +82,12 @@ __device__ __forceinline__ void build_cand(const Cand &cd, CandSmem cs, int Px, 
 #pragma unroll
         for (int o = 0; o < 8; ++o) {
             const int sx = (o & 1) ? -1 : 1, sy = (o & 2) ? -1 : 1, sz = (o & 4) ? -1 : 1;
-            cs.off[i * 8 + o] = sz * dz * PxPy + sy * dy * Px + sx * dx;
+            cs.off[o * cs.stride + i] = sz * dz * PxPy + sy * dy * Px + sx * dx;
         }
     }
 }
 
-size_t cand_smem_bytes(int n) { return (size_t)n * (sizeof(float4) + 8 * sizeof(int)); }
+size_t cand_smem_bytes(int n) { return (size_t)n * sizeof(float4) + (size_t)8 * cand_stride(n) * sizeof(int); }
 
 // Per-sample reflected coordinates.
 struct SampleGeo {
@@ -112,7 +127,7 @@ __device__ __forceinline__ bool tap(int ci, const SampleGeo &g, const CandSmem &
         if (!(ex2 <= h2 && ey2 <= h2 && ez2 <= h2)) return false;
         w = kb_weight(ez2, kb) * kb_weight(ey2, kb) * kb_weight(ex2, kb);
     }
-    off = g.base + cs.off[ci * 8 + g.oct];
+    off = g.base + cs.off[g.oct * cs.stride + ci];
     return true;
 }
 
@@ -216,9 +231,7 @@ __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2
     constexpr int pv = Plane<R>::PS;
     const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
     CandSmem cs;
-    cs.f = smem4;
-    cs.off = reinterpret_cast<int *>(smem4 + cd.n);
-    float2 *tile = reinterpret_cast<float2 *>(cs.off + 8 * cd.n);
+    float2 *tile = reinterpret_cast<float2 *>(carve_cand(cd, cs, smem4));
     const int tid = bi.x;
     const int tx = tid % g.nt[0];
     const int ty = (tid / g.nt[0]) % g.nt[1];
@@ -347,9 +360,7 @@ __device__ __forceinline__ void spread_body(const float2 *__restrict__ ks, float
     constexpr int ps = IPlane<R>::PS;
     const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
     CandSmem cs;
-    cs.f = smem4;
-    cs.off = reinterpret_cast<int *>(smem4 + cd.n);
-    int *tile = reinterpret_cast<int *>(smem4 + cd.n + 2 * cd.n);
+    int *tile = reinterpret_cast<int *>(carve_cand(cd, cs, smem4));
     const int tid = bi.x;
     const int tx = tid % g.nt[0];
     const int ty = (tid / g.nt[0]) % g.nt[1];
@@ -459,9 +470,7 @@ k_weight_sum(const float4 *__restrict__ samples, int4 *__restrict__ blocks, Geom
     const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
     const int pv = PxPy * g.P[2];
     CandSmem cs;
-    cs.f = smem4;
-    cs.off = reinterpret_cast<int *>(smem4 + cd.n);
-    float *tile = reinterpret_cast<float *>(smem4 + cd.n + 2 * cd.n);
+    float *tile = reinterpret_cast<float *>(carve_cand(cd, cs, smem4));
     const int4 bi = blocks[blockIdx.x];
     for (int t = threadIdx.x; t < pv; t += blockDim.x) tile[t] = 0.f;
     build_cand(cd, cs, Px, PxPy);

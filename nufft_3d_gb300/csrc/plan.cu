@@ -86,6 +86,50 @@ static double kernel_host(double dist2, double alpha, double J)
     return (bessi0c(arg) / den).real();
 }
 
+// Polynomial in t = 1 - dist2/(J/2)^2 for the kernel on its support
+// (kernel.m:2-11 with t in [0, 1]): interpolation at the kKBDeg+1 Chebyshev
+// nodes of [0, 1], converted to monomial coefficients in t, all in FP64.  The
+// FP32 Horner evaluation is then emulated on a fine grid against the FP64
+// kernel; the fit is used only if its largest error stays below 1e-6 (true
+// for the usual alpha; very large alpha keeps the direct evaluation).
+static void fit_kb_poly(double alpha, double i0a, KBParams &kb)
+{
+    constexpr int n = kKBDeg + 1;
+    double f[n], c[n];
+    for (int j = 0; j < n; ++j) {
+        const double x = std::cos(M_PI * (j + 0.5) / n), t = 0.5 * (x + 1);
+        f[j] = bessi0_host(alpha * std::sqrt(t)) / i0a;
+    }
+    for (int k = 0; k < n; ++k) {
+        double a = 0;
+        for (int j = 0; j < n; ++j) a += f[j] * std::cos(M_PI * k * (j + 0.5) / n);
+        c[k] = a * 2.0 / n;
+    }
+    c[0] *= 0.5;
+    // sum_k c_k T_k(2t - 1) in powers of t: T_{k+1} = 2 (2t - 1) T_k - T_{k-1}
+    std::vector<double> m(n, 0.0), tkm1(n, 0.0), tk(n, 0.0), tkp1(n, 0.0);
+    tkm1[0] = 1;
+    tk[0] = -1;
+    tk[1] = 2;
+    m[0] = c[0];
+    for (int i = 0; i < n; ++i) m[i] += c[1] * tk[i];
+    for (int k = 1; k + 1 < n; ++k) {
+        for (int i = 0; i < n; ++i) tkp1[i] = -2 * tk[i] - tkm1[i] + (i > 0 ? 4 * tk[i - 1] : 0.0);
+        for (int i = 0; i < n; ++i) m[i] += c[k + 1] * tkp1[i];
+        tkm1.swap(tk);
+        tk.swap(tkp1);
+    }
+    for (int i = 0; i < n; ++i) kb.c[i] = (float)m[i];
+    double err = 0;
+    for (int i = 0; i <= 8192; ++i) {
+        const float t = (float)(i / 8192.0);
+        float s = kb.c[kKBDeg];
+        for (int k = kKBDeg - 1; k >= 0; --k) s = std::fma(s, t, kb.c[k]);
+        err = std::max(err, std::fabs((double)s - bessi0_host(alpha * std::sqrt((double)t)) / i0a));
+    }
+    kb.poly = err < 1e-6 ? 1 : 0;
+}
+
 // deap.m:2-36,97-98.  ifft(X*K, 2K, 'symmetric') of the (J+1)-sample kernel
 // table is 0.5*T0 + sum_{d>=1} T_d cos(pi d m / K); rows m in [-N/2, N/2) are
 // kept and fftshifted, so output index p holds m = p - N/2.  Returns 1/U.
@@ -702,6 +746,7 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
     kb.inv_i0a = (float)(1.0 / p->i0a);
     kb.exp_over_i0a = (float)(std::exp(alpha) / p->i0a);
     kb.half2 = (float)(half * half);
+    fit_kb_poly(alpha, p->i0a, kb);
     int cpp = o.max_coils_per_pass > 0 ? o.max_coils_per_pass : 8;
     int cb = 1;
     while (cb * 2 <= cpp && cb < 8) cb *= 2;
