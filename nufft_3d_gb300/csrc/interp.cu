@@ -131,6 +131,30 @@ __device__ __forceinline__ bool tap(int ci, const SampleGeo &g, const CandSmem &
     return true;
 }
 
+// Branch-free form of tap for the hot loops: the candidate index is clamped
+// into the list (so every load stays inside the tables and the tile) and the
+// weight is computed for every lane; the returned flag says whether the
+// candidate exists and lies inside the support.
+template <bool RADIAL>
+__device__ __forceinline__ bool tap_all(int ci, int n, const SampleGeo &g, const CandSmem &cs,
+                                        const KBParams &kb, float &w, int &off)
+{
+    const bool valid = ci < n;
+    const int cc = valid ? ci : n - 1;
+    const float4 cf = cs.f[cc];
+    off = g.base + cs.off[g.oct * cs.stride + cc];
+    const float ex = cf.x - g.fx, ey = cf.y - g.fy, ez = cf.z - g.fz;
+    const float ex2 = ex * ex, ey2 = ey * ey, ez2 = ez * ez;
+    const float h2 = kb.half2;
+    if (RADIAL) {
+        const float d2 = ez2 + ey2 + ex2;
+        w = kb_weight(d2, kb);
+        return valid && d2 <= h2;
+    }
+    w = kb_weight(ez2, kb) * kb_weight(ey2, kb) * kb_weight(ex2, kb);
+    return valid && ex2 <= h2 && ey2 <= h2 && ez2 <= h2;
+}
+
 // Visit every (tile point, coil) of the padded tile with the grid point it
 // maps to: warps take tile rows (one division per row), lanes run along x and
 // the coil index (V values per point) so global accesses stay contiguous.
@@ -186,7 +210,7 @@ __device__ __forceinline__ int eval_chunk(int base, const SampleGeo &sg, const C
     const int ci = base + lane;
     float w = 0.f;
     int off = 0;
-    const bool hit = ci < ncand && tap<RADIAL>(ci, sg, cs, kb, w, off);
+    const bool hit = tap_all<RADIAL>(ci, ncand, sg, cs, kb, w, off);
     const unsigned m = __ballot_sync(0xffffffffu, hit);
     if (hit) {
         const int r = __popc(m & ((1u << lane) - 1u));
@@ -202,6 +226,8 @@ __device__ __forceinline__ int eval_chunk(int base, const SampleGeo &sg, const C
 // acc[c] += w * tile(c, off): coil pairs come from one 16-byte load of a pair
 // plane; a quarter-warp is one sample's chunk of 8 candidates, whose tile
 // words the plan-time candidate order spreads over distinct bank groups.
+// acc[c] += w * tile(c, off): coil pairs come from one 16-byte load of a pair
+// plane.
 template <int CB, int PV>
 __device__ __forceinline__ void accumulate(float2 (&acc)[CB], const float2 *tile, int off, float w)
 {
@@ -271,6 +297,7 @@ __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2
             const int ci0 = it * kGroup + lig, ci1 = ci0 + kGroup;
             float w0, w1;
             int off0, off1;
+            // (branchy form: a branch-free variant with predicated loads was slower here)
             const bool h0 = ci0 < cd.n && tap<RADIAL>(ci0, sg, cs, kb, w0, off0);
             const bool h1 = ci1 < cd.n && tap<RADIAL>(ci1, sg, cs, kb, w1, off1);
             if (h0) accumulate<CB, pv>(acc, tile, off0, w0);
