@@ -24,8 +24,10 @@ struct BankOrderStats {
     double spread_before, spread_after;
 };
 
+// lo/hi: the box of reflected offsets |f| the list serves (per axis).
 inline void bank_order(std::vector<int> &code, int Px, int PxPy, double J, int radial, int is2d,
-                       BankOrderStats *stats = nullptr, int n_samples = 192, int sweeps = 40)
+                       const double lo[3], const double hi[3], BankOrderStats *stats = nullptr,
+                       int n_samples = 160, int sweeps = 24)
 {
     const int n = (int)code.size();
     if (n <= 8) return;
@@ -44,9 +46,8 @@ inline void bank_order(std::vector<int> &code, int Px, int PxPy, double J, int r
         double f[3];
         int sg[3];
         for (int a = 0; a < 3; ++a) {
-            const double v = uni() - 0.5;
-            sg[a] = v < 0 ? -1 : 1;
-            f[a] = v < 0 ? -v : v;
+            sg[a] = uni() < 0.5 ? -1 : 1;
+            f[a] = lo[a] + (hi[a] - lo[a]) * uni();
         }
         if (is2d) {
             f[2] = 0;

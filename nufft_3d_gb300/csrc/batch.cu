@@ -514,8 +514,7 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             d.blocks = p->blocks;
             d.g = p->geom;
             d.kb = p->kb;
-            d.cand = p->cand;
-            d.n_cand = p->n_cand;
+            d.cand = p->cand_desc;
             d.nc = nc[v];
             b->h_gat[v] = d;
             b->h_spr[v] = d;

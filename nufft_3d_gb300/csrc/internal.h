@@ -152,6 +152,15 @@ struct BatchFFT {
     FFTDesc fd;
 };
 
+// Candidate taps of a plan (see the interpolation kernels): packed offsets
+// (dx'+8) | (dy'+8)<<4 | (dz'+8)<<8 of the 8 sub-cube lists back to back.
+struct Cand {
+    const int *list;
+    int n;          // total entries
+    int start[8];   // first entry of sub-cube q's list
+    int cnt[8];     // its length
+};
+
 struct BatchInterp {
     const float2 *in;   // gather: grid; spread: sorted samples
     float2 *out;        // gather: sorted samples; spread: grid
@@ -160,8 +169,7 @@ struct BatchInterp {
     const float *wsample;
     Geom g;
     KBParams kb;
-    const int *cand;
-    int n_cand;
+    Cand cand;
     int nc;
     float scale;
 };
@@ -258,7 +266,8 @@ struct nufft3d_plan {
     int32_t *inv = nullptr;     // original -> sorted, -1 out of bounds
     int4 *blocks = nullptr;     // (tile, start, count, float bits of max summed weight)
     int *cand = nullptr;        // candidate tap offsets (reflected octant), packed
-    int n_cand = 0;
+    int n_cand = 0;             // total entries of the 8 sub-cube lists
+    nufft3d::Cand cand_desc{};         // device list + per-sub-cube starts and lengths
     int64_t n_blocks = 0;
     int coils_per_pass = 8;
     int threads = 256;

@@ -41,81 +41,89 @@ __device__ __forceinline__ int wrap_idx(int x, int K)
     return x < 0 ? x + K : x;
 }
 
-// Candidate tap offsets, reflected into the octant f >= 0: packed
-// (dx+8) | (dy+8)<<4 | (dz+8)<<8, sorted so taps kept for every f come first.
-// A sample with fractional offset f uses offset s*d' where s = sign(f) per
-// axis and tests (d' - |f|)^2 per axis -- the same value as (s*d' - f)^2.
-struct Cand {
-    const int *list;
-    int n;
-};
-
-// Per-block candidate tables in shared memory: offsets as floats for the
-// distance test and the tile offset of each candidate in each of the 8 sign
-// octants, octant-major so that lanes reading consecutive candidates of one
-// octant hit consecutive banks; the octant stride is 8 mod 32 so that lane
-// groups reading the same candidates in different octants shift banks.
+// Candidate taps (struct Cand, built at plan time): a sample's fractional
+// offset f from its rounded grid point is reflected into the octant
+// |f| in [0, 1/2]^3, which is split into 8 sub-cubes (|f_a| below or above
+// 1/4 per axis); each sub-cube has its own list of offsets d' that can fall
+// inside the support.  A sample uses the tap s*d' (s = sign(f) per axis) and
+// tests (d' - |f|)^2 per axis -- the same value as (s*d' - f)^2.
+//
+// Per-block copy in shared memory: the 8 list starts and lengths, then every
+// offset as floats (dx', dy', dz', 0).  The tile offset of a tap is computed
+// from the sample's signed strides, so no per-octant table is needed.
 struct CandSmem {
-    float4 *f;   // [n] (dx', dy', dz', 0)
-    int *off;    // [8][stride]
-    int stride;
+    const int *sc;  // [16]: start[8], cnt[8]
+    float4 *f;      // [n]
 };
-
-__host__ __device__ __forceinline__ int cand_stride(int n) { return n + ((8 - n % 32) + 32) % 32; }
 
 // Candidate tables at the start of the dynamic shared memory; returns the
 // first free 16-byte word after them.
 __device__ __forceinline__ float4 *carve_cand(const Cand &cd, CandSmem &cs, float4 *smem4)
 {
-    cs.stride = cand_stride(cd.n);
-    cs.f = smem4;
-    cs.off = reinterpret_cast<int *>(smem4 + cd.n);
-    return smem4 + cd.n + 2 * cs.stride;
+    cs.sc = reinterpret_cast<const int *>(smem4);
+    cs.f = smem4 + 4;
+    return smem4 + 4 + cd.n;
 }
 
-__device__ __forceinline__ void build_cand(const Cand &cd, CandSmem cs, int Px, int PxPy)
+__device__ __forceinline__ void build_cand(const Cand &cd, CandSmem cs)
 {
+    int *sc = const_cast<int *>(cs.sc);
+    if (threadIdx.x < 8) {
+        sc[threadIdx.x] = cd.start[threadIdx.x];
+        sc[8 + threadIdx.x] = cd.cnt[threadIdx.x];
+    }
     for (int i = threadIdx.x; i < cd.n; i += blockDim.x) {
         const int code = cd.list[i];
         const int dx = (code & 15) - 8, dy = ((code >> 4) & 15) - 8, dz = ((code >> 8) & 15) - 8;
         cs.f[i] = make_float4((float)dx, (float)dy, (float)dz, 0.f);
-#pragma unroll
-        for (int o = 0; o < 8; ++o) {
-            const int sx = (o & 1) ? -1 : 1, sy = (o & 2) ? -1 : 1, sz = (o & 4) ? -1 : 1;
-            cs.off[o * cs.stride + i] = sz * dz * PxPy + sy * dy * Px + sx * dx;
-        }
     }
 }
 
-size_t cand_smem_bytes(int n) { return (size_t)n * sizeof(float4) + (size_t)8 * cand_stride(n) * sizeof(int); }
+size_t cand_smem_bytes(int n) { return (size_t)(n + 4) * sizeof(float4); }
 
 // Per-sample reflected coordinates.
 struct SampleGeo {
     float fx, fy, fz;  // |f|
-    int oct;           // sign octant: bit0 x<0, bit1 y<0, bit2 z<0
-    int base;          // tile-local index of the rounded position
+    float sx, sy, sz;  // signed tile strides of the sample's octant: +-1, +-Px, +-Px*Py
+    float b;           // tile index of the rounded position + 1.5*2^23 (see tap)
+    int lbase, ln;     // the sample's sub-cube candidate list
 };
 
-__device__ __forceinline__ SampleGeo sample_geo(const float4 rec, int Px, int Py)
+// Reads the list starts and lengths from shared memory: call after the
+// barrier that follows build_cand.
+__device__ __forceinline__ SampleGeo sample_geo(const float4 rec, int Px, int Py, const CandSmem &cs)
 {
     SampleGeo g;
     const int packed = __float_as_int(rec.w);
     const int lx0 = packed & 0xFF, ly0 = (packed >> 8) & 0xFF, lz0 = (packed >> 16) & 0xFF;
-    g.oct = (rec.x < 0.f ? 1 : 0) | (rec.y < 0.f ? 2 : 0) | (rec.z < 0.f ? 4 : 0);
+    g.sx = rec.x < 0.f ? -1.f : 1.f;
+    g.sy = rec.y < 0.f ? (float)-Px : (float)Px;
+    g.sz = rec.z < 0.f ? (float)(-Px * Py) : (float)(Px * Py);
     g.fx = fabsf(rec.x);
     g.fy = fabsf(rec.y);
     g.fz = fabsf(rec.z);
-    g.base = (lz0 * Py + ly0) * Px + lx0;
+    g.b = (float)((lz0 * Py + ly0) * Px + lx0) + 12582912.0f;
+    const int q = (g.fx >= 0.25f ? 1 : 0) | (g.fy >= 0.25f ? 2 : 0) | (g.fz >= 0.25f ? 4 : 0);
+    g.lbase = cs.sc[q];
+    g.ln = cs.sc[8 + q];
     return g;
 }
 
-// Weight and tile offset of candidate ci for a sample; false outside the
-// kernel support (the neighbour test of nufft_3d.m:183-192).
+// Tile offset of the candidate with reflected offset cf: base + s*d' summed
+// in floating point on top of 1.5*2^23, where every partial sum is an exact
+// integer (|values| < 2^22), read back from the bits.
+__device__ __forceinline__ int tap_offset(const float4 cf, const SampleGeo &g)
+{
+    return __float_as_int(fmaf(cf.z, g.sz, fmaf(cf.y, g.sy, fmaf(cf.x, g.sx, g.b)))) - 0x4B400000;
+}
+
+// Weight and tile offset of candidate ci (< g.ln) of the sample's list; false
+// outside the kernel support (the neighbour test of nufft_3d.m:183-192).
 template <bool RADIAL>
 __device__ __forceinline__ bool tap(int ci, const SampleGeo &g, const CandSmem &cs, const KBParams &kb,
                                     float &w, int &off)
 {
-    const float4 cf = cs.f[ci];
+    const float4 cf = cs.f[g.lbase + ci];
     const float ex = cf.x - g.fx, ey = cf.y - g.fy, ez = cf.z - g.fz;
     const float ex2 = ex * ex, ey2 = ey * ey, ez2 = ez * ez;
     const float h2 = kb.half2;
@@ -127,7 +135,7 @@ __device__ __forceinline__ bool tap(int ci, const SampleGeo &g, const CandSmem &
         if (!(ex2 <= h2 && ey2 <= h2 && ez2 <= h2)) return false;
         w = kb_weight(ez2, kb) * kb_weight(ey2, kb) * kb_weight(ex2, kb);
     }
-    off = g.base + cs.off[g.oct * cs.stride + ci];
+    off = tap_offset(cf, g);
     return true;
 }
 
@@ -136,13 +144,13 @@ __device__ __forceinline__ bool tap(int ci, const SampleGeo &g, const CandSmem &
 // weight is computed for every lane; the returned flag says whether the
 // candidate exists and lies inside the support.
 template <bool RADIAL>
-__device__ __forceinline__ bool tap_all(int ci, int n, const SampleGeo &g, const CandSmem &cs,
-                                        const KBParams &kb, float &w, int &off)
+__device__ __forceinline__ bool tap_all(int ci, const SampleGeo &g, const CandSmem &cs, const KBParams &kb,
+                                        float &w, int &off)
 {
-    const bool valid = ci < n;
-    const int cc = valid ? ci : n - 1;
-    const float4 cf = cs.f[cc];
-    off = g.base + cs.off[g.oct * cs.stride + cc];
+    const bool valid = ci < g.ln;
+    const int cc = valid ? ci : g.ln - 1;
+    const float4 cf = cs.f[g.lbase + cc];
+    off = tap_offset(cf, g);
     const float ex = cf.x - g.fx, ey = cf.y - g.fy, ez = cf.z - g.fz;
     const float ex2 = ex * ex, ey2 = ey * ey, ez2 = ez * ez;
     const float h2 = kb.half2;
@@ -204,13 +212,13 @@ struct TapQueue {
 // Evaluate candidates [base, base+32) of sample sg; returns the number of hits
 // written to the warp's queue (in lane order).
 template <bool RADIAL>
-__device__ __forceinline__ int eval_chunk(int base, const SampleGeo &sg, const CandSmem &cs, int ncand,
+__device__ __forceinline__ int eval_chunk(int base, const SampleGeo &sg, const CandSmem &cs,
                                           const KBParams &kb, TapQueue &qu, int lane)
 {
     const int ci = base + lane;
     float w = 0.f;
     int off = 0;
-    const bool hit = tap_all<RADIAL>(ci, ncand, sg, cs, kb, w, off);
+    const bool hit = tap_all<RADIAL>(ci, sg, cs, kb, w, off);
     const unsigned m = __ballot_sync(0xffffffffu, hit);
     if (hit) {
         const int r = __popc(m & ((1u << lane) - 1u));
@@ -276,19 +284,19 @@ __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2
         }
     });
     asm volatile("cp.async.commit_group;" ::: "memory");
-    build_cand(cd, cs, Px, PxPy);
+    build_cand(cd, cs);
     asm volatile("cp.async.wait_all;" ::: "memory");
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const int lig = lane & (kGroup - 1);
     const unsigned gmask = 0xFFu << (lane & ~(kGroup - 1));
     const int grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
-    const int niter = (cd.n + kGroup - 1) / kGroup;
     const int send = bi.y + bi.z;
     float4 rec_next = bi.y + grp < send ? __ldg(&samples[bi.y + grp]) : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int s = bi.y + grp; s < send; s += ngrp) {
-        const SampleGeo sg = sample_geo(rec_next, Px, g.P[1]);
+        const SampleGeo sg = sample_geo(rec_next, Px, g.P[1], cs);
         if (s + ngrp < send) rec_next = __ldg(&samples[s + ngrp]);
+        const int niter = (sg.ln + kGroup - 1) / kGroup;
         float2 acc[CB];
 #pragma unroll
         for (int c = 0; c < CB; ++c) acc[c] = make_float2(0.f, 0.f);
@@ -298,8 +306,8 @@ __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2
             float w0, w1;
             int off0, off1;
             // (branchy form: a branch-free variant with predicated loads was slower here)
-            const bool h0 = ci0 < cd.n && tap<RADIAL>(ci0, sg, cs, kb, w0, off0);
-            const bool h1 = ci1 < cd.n && tap<RADIAL>(ci1, sg, cs, kb, w1, off1);
+            const bool h0 = ci0 < sg.ln && tap<RADIAL>(ci0, sg, cs, kb, w0, off0);
+            const bool h1 = ci1 < sg.ln && tap<RADIAL>(ci1, sg, cs, kb, w1, off1);
             if (h0) accumulate<CB, pv>(acc, tile, off0, w0);
             if (h1) accumulate<CB, pv>(acc, tile, off1, w1);
         }
@@ -404,7 +412,7 @@ __device__ __forceinline__ void spread_body(const float2 *__restrict__ ks, float
         }
     }
     for (int t = threadIdx.x; t < ps * CB * 2; t += blockDim.x) tile[t] = 0;
-    build_cand(cd, cs, Px, PxPy);
+    build_cand(cd, cs);
     const float ymax = block_max(m, red);   // contains __syncthreads
     if (!(ymax > 0.f)) return;             // nothing to add (block-uniform)
     const float wsum = fmaxf(__int_as_float(bi.w), 1.0f);
@@ -430,14 +438,14 @@ __device__ __forceinline__ void spread_body(const float2 *__restrict__ ks, float
         load_y(bi.y + warp, y_next);
     }
     for (int s = bi.y + warp; s < send; s += nwarps) {
-        const SampleGeo sg = sample_geo(rec_next, Px, g.P[1]);
+        const SampleGeo sg = sample_geo(rec_next, Px, g.P[1], cs);
         const float4 y = y_next;
         if (s + nwarps < send) {
             rec_next = __ldg(&samples[s + nwarps]);
             load_y(s + nwarps, y_next);
         }
-        for (int base = 0; base < cd.n; base += 32) {
-            const int nh = eval_chunk<RADIAL>(base, sg, cs, cd.n, kb, qu, lane);
+        for (int base = 0; base < sg.ln; base += 32) {
+            const int nh = eval_chunk<RADIAL>(base, sg, cs, kb, qu, lane);
             for (int t = j; t < nh; t += CPS) {
                 const float w = qu.w[t];
                 const int off = qu.off[t];
@@ -500,18 +508,16 @@ k_weight_sum(const float4 *__restrict__ samples, int4 *__restrict__ blocks, Geom
     float *tile = reinterpret_cast<float *>(carve_cand(cd, cs, smem4));
     const int4 bi = blocks[blockIdx.x];
     for (int t = threadIdx.x; t < pv; t += blockDim.x) tile[t] = 0.f;
-    build_cand(cd, cs, Px, PxPy);
+    build_cand(cd, cs);
     __syncthreads();
     const int lig = threadIdx.x & (kGroup - 1);
     const int grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
-    const int niter = (cd.n + kGroup - 1) / kGroup;
     for (int s = bi.y + grp; s < bi.y + bi.z; s += ngrp) {
-        const SampleGeo sg = sample_geo(__ldg(&samples[s]), Px, g.P[1]);
-        for (int it = 0; it < niter; ++it) {
-            const int ci = it * kGroup + lig;
+        const SampleGeo sg = sample_geo(__ldg(&samples[s]), Px, g.P[1], cs);
+        for (int ci = lig; ci < sg.ln; ci += kGroup) {
             float w;
             int off;
-            if (ci < cd.n && tap<RADIAL>(ci, sg, cs, kb, w, off)) atomicAdd(&tile[off], w);
+            if (tap<RADIAL>(ci, sg, cs, kb, w, off)) atomicAdd(&tile[off], w);
         }
     }
     __syncthreads();
@@ -565,7 +571,7 @@ k_gather_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ ta
     extern __shared__ float4 smem4[];
     const int4 e = table[blockIdx.x];
     const BatchInterp &b = vols[e.x];
-    const Cand cd{b.cand, b.n_cand};
+    const Cand &cd = b.cand;
     gather_body<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, b.kb, b.scale, b.wsample,
                                cd, smem4);
 }
@@ -579,7 +585,7 @@ k_spread_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ ta
     __shared__ TapQueue queues[kInterpThreads / 32];
     const int4 e = table[blockIdx.x];
     const BatchInterp &b = vols[e.x];
-    const Cand cd{b.cand, b.n_cand};
+    const Cand &cd = b.cand;
     spread_body<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, b.kb, cd, smem4, red,
                                queues);
 }
@@ -619,7 +625,7 @@ size_t smem_interp_bytes(const Geom &g, int cb)
     return (size_t)g.P[0] * g.P[1] * g.P[2] * cb * sizeof(float2);
 }
 
-static Cand cand_of(const nufft3d_plan *p) { return Cand{p->cand, p->n_cand}; }
+static const Cand &cand_of(const nufft3d_plan *p) { return p->cand_desc; }
 
 size_t smem_plane_bytes(int R, int cb)
 {

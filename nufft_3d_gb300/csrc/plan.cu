@@ -195,17 +195,25 @@ static std::vector<double> deap_host(const int N[3], const int K[3], double J, d
     return U;
 }
 
-// Candidate taps for the octant f in [0, 1/2]^3 (samples are reflected onto
-// it): offsets d' in [-R, R]^3 whose smallest possible distance over that
-// octant is inside the support, ordered near to far (offsets inside the
-// support for every f first; bank_order then re-partitions nearby chunks of 8
-// for shared-memory banks).  A relative slack of 1e-5 keeps every tap that the
-// single-precision test in the kernels can accept.
-static std::vector<int> make_candidates(int R, int radial, int is2d, double J)
+// Candidate taps for the box lo <= f <= hi (per axis) inside the reflected
+// octant [0, 1/2]^3: offsets d' in [-R, R]^3 whose smallest possible distance
+// over the box is inside the support, ordered near to far (offsets inside the
+// support for every f of the box first; bank_order then re-partitions nearby
+// chunks of 8 for shared-memory banks).  A relative slack of 1e-5 keeps every
+// tap that the single-precision test in the kernels can accept.
+static std::vector<int> make_candidates(int R, int radial, int is2d, double J, const double lo[3],
+                                        const double hi[3])
 {
     const double h2 = (J / 2) * (J / 2) * (1 + 1e-5);
-    auto mn = [](int d) { return d <= 0 ? double(d) * d : (d - 0.5) * (d - 0.5); };
-    auto mx = [](int d) { return d >= 0.25 ? double(d) * d : (d - 0.5) * (d - 0.5); };
+    auto mn = [&](int d, int a) {
+        if (d >= lo[a] && d <= hi[a]) return 0.0;
+        const double u = d - lo[a], v = d - hi[a];
+        return std::min(u * u, v * v);
+    };
+    auto mx = [&](int d, int a) {
+        const double u = d - lo[a], v = d - hi[a];
+        return std::max(u * u, v * v);
+    };
     struct C {
         double key, key2;
         int code;
@@ -215,16 +223,11 @@ static std::vector<int> make_candidates(int R, int radial, int is2d, double J)
     for (int dz = -rz; dz <= rz; ++dz)
         for (int dy = -R; dy <= R; ++dy)
             for (int dx = -R; dx <= R; ++dx) {
-                bool keep;
-                double key;
-                if (radial) {
-                    keep = mn(dx) + mn(dy) + mn(dz) <= h2;
-                    key = mx(dx) + mx(dy) + mx(dz);
-                } else {
-                    keep = mn(dx) <= h2 && mn(dy) <= h2 && mn(dz) <= h2;
-                    key = std::max(mx(dx), std::max(mx(dy), mx(dz)));
-                }
-                if (keep) v.push_back({key, mn(dx) + mn(dy) + mn(dz), (dx + 8) | ((dy + 8) << 4) | ((dz + 8) << 8)});
+                const double n0 = mn(dx, 0), n1 = mn(dy, 1), n2 = mn(dz, 2);
+                const double x0 = mx(dx, 0), x1 = mx(dy, 1), x2 = mx(dz, 2);
+                const bool keep = radial ? n0 + n1 + n2 <= h2 : (n0 <= h2 && n1 <= h2 && n2 <= h2);
+                const double key = radial ? x0 + x1 + x2 : std::max(x0, std::max(x1, x2));
+                if (keep) v.push_back({key, n0 + n1 + n2, (dx + 8) | ((dy + 8) << 4) | ((dz + 8) << 8)});
             }
     std::stable_sort(v.begin(), v.end(), [](const C &a, const C &b) {
         return a.key != b.key ? a.key < b.key : a.key2 < b.key2;
@@ -234,19 +237,38 @@ static std::vector<int> make_candidates(int R, int radial, int is2d, double J)
     return out;
 }
 
-// make_candidates + bank_order, cached per geometry (the search takes ~0.1 s)
-static std::vector<int> ordered_candidates(int R, int radial, int is2d, double J, int Px, int PxPy)
+// The 8 sub-cube lists of the reflected octant (sub-cube q: |f_a| >= 1/4
+// iff bit a of q), each ordered by bank_order, back to back.  Cached per
+// geometry: the ordering search takes a fraction of a second.
+struct CandSet {
+    std::vector<int> codes;
+    int start[8], cnt[8];
+};
+
+static const CandSet &candidate_set(int R, int radial, int is2d, double J, int Px, int PxPy)
 {
     static std::mutex mu;
-    static std::map<std::tuple<int, int, int, double, int, int>, std::vector<int>> cache;
+    static std::map<std::tuple<int, int, int, double, int, int>, CandSet> cache;
     const auto key = std::make_tuple(R, radial, is2d, J, Px, PxPy);
     std::lock_guard<std::mutex> lk(mu);
     auto it = cache.find(key);
     if (it != cache.end()) return it->second;
-    std::vector<int> c = make_candidates(R, radial, is2d, J);
-    bank_order(c, Px, PxPy, J, radial, is2d);
-    cache.emplace(key, c);
-    return c;
+    CandSet cs;
+    for (int q = 0; q < 8; ++q) {
+        double lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            const bool up = (q >> a) & 1;
+            lo[a] = up ? 0.25 : 0.0;
+            hi[a] = up ? 0.5 : 0.25;
+        }
+        if (is2d) lo[2] = hi[2] = 0.0;  // f_z = 0 in 2-D
+        std::vector<int> c = make_candidates(R, radial, is2d, J, lo, hi);
+        bank_order(c, Px, PxPy, J, radial, is2d, lo, hi);
+        cs.start[q] = (int)cs.codes.size();
+        cs.cnt[q] = (int)c.size();
+        cs.codes.insert(cs.codes.end(), c.begin(), c.end());
+    }
+    return cache.emplace(key, std::move(cs)).first->second;
 }
 
 // ------------------------------------------------------ device kernels
@@ -578,11 +600,17 @@ static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts
     }
 
     {
-        std::vector<int> cand = ordered_candidates(g.R, g.radial, g.is2d, p->J, g.P[0], g.P[0] * g.P[1]);
-        if (cand.size() > 512) return fail(NUFFT3D_ERR_UNSUPPORTED, "too many candidate taps");
-        p->n_cand = (int)cand.size();
-        NUFFT_TRY(dmalloc(&p->cand, cand.size(), &p->table_bytes));
-        NUFFT_CUDA_TRY(cudaMemcpyAsync(p->cand, cand.data(), sizeof(int) * cand.size(), cudaMemcpyHostToDevice, s));
+        const CandSet &cs = candidate_set(g.R, g.radial, g.is2d, p->J, g.P[0], g.P[0] * g.P[1]);
+        p->n_cand = (int)cs.codes.size();
+        NUFFT_TRY(dmalloc(&p->cand, cs.codes.size(), &p->table_bytes));
+        NUFFT_CUDA_TRY(
+            cudaMemcpyAsync(p->cand, cs.codes.data(), sizeof(int) * cs.codes.size(), cudaMemcpyHostToDevice, s));
+        p->cand_desc.list = p->cand;
+        p->cand_desc.n = p->n_cand;
+        for (int q = 0; q < 8; ++q) {
+            p->cand_desc.start[q] = cs.start[q];
+            p->cand_desc.cnt[q] = cs.cnt[q];
+        }
     }
     NUFFT_TRY(launch_weight_sum(p, s));
     // deapodization (FP64 on the host, stored FP32 like deap.m:100-101)
@@ -750,8 +778,9 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
     int cpp = o.max_coils_per_pass > 0 ? o.max_coils_per_pass : 8;
     int cb = 1;
     while (cb * 2 <= cpp && cb < 8) cb *= 2;
-    // the kernels also hold the candidate tables (<= 461 taps for R <= 4)
-    const size_t cand_max = cand_smem_bytes(R <= 2 ? 128 : (R == 3 ? 256 : 512));
+    // the kernels also hold the candidate tables
+    const size_t cand_max =
+        cand_smem_bytes((int)candidate_set(R, g.radial, is2d, o.J, g.P[0], g.P[0] * g.P[1]).codes.size());
     while (cb > 1 && smem_plane_bytes(R, cb) + cand_max > 210 * 1024) cb /= 2;
     if (smem_plane_bytes(R, cb) + cand_max > 220 * 1024) {
         delete p;
@@ -806,6 +835,7 @@ extern "C" int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **out)
     p->n_blocks = src->n_blocks;
     p->cand = src->cand;
     p->n_cand = src->n_cand;
+    p->cand_desc = src->cand_desc;
     p->coils_per_pass = src->coils_per_pass;
     p->taps = src->taps;
     p->U = src->U;
