@@ -406,6 +406,7 @@ extern "C" int nufft3d_forward_host(nufft3d_plan *p, const float *x, float *k, i
     NUFFT_TRY(op_forward(p, (const float2 *)p->stage.in, (float2 *)p->stage.out, nc, s));
     NUFFT_CUDA_TRY(cudaMemcpyAsync(k, p->stage.out, bo, cudaMemcpyDeviceToHost, s));
     NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    NUFFT_TRY(interp_check_error());
     return NUFFT3D_SUCCESS;
 }
 
@@ -421,6 +422,7 @@ extern "C" int nufft3d_adjoint_host(nufft3d_plan *p, const float *k, float *x, i
     NUFFT_TRY(op_adjoint(p, (const float2 *)p->stage.in, (float2 *)p->stage.out, nc, s));
     NUFFT_CUDA_TRY(cudaMemcpyAsync(x, p->stage.out, bo, cudaMemcpyDeviceToHost, s));
     NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    NUFFT_TRY(interp_check_error());
     return NUFFT3D_SUCCESS;
 }
 
@@ -432,6 +434,7 @@ extern "C" int nufft3d_density(nufft3d_plan *p, int maxit)
     DevGuard g(p->device);
     NUFFT_TRY(run_density(p, maxit, p->own_stream));
     NUFFT_CUDA_TRY(cudaStreamSynchronize(p->own_stream));
+    NUFFT_TRY(interp_check_error());
     return NUFFT3D_SUCCESS;
 }
 

@@ -531,7 +531,7 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             ig.n = (int)tab.size();
             const size_t plane = smem_plane_bytes(b->R, w);
             const size_t iplane = (size_t)(((plane / (w * sizeof(float2)) + 29) / 32) * 32 + 2) * w * 2 * sizeof(int);
-            ig.smem = std::max(plane, iplane) + cand_smem_bytes(maxcand);
+            ig.smem = std::max(plane, iplane) + cand_smem_bytes(maxcand) + 128;  // + tile alignment
             int s2 = dalloc(b, &ig.tab, tab.size());
             if (s2 != NUFFT3D_SUCCESS) return bail(s2);
             if (cudaMemcpy(ig.tab, tab.data(), tab.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess)

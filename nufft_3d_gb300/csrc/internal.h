@@ -270,6 +270,7 @@ struct nufft3d_plan {
     nufft3d::Cand cand_desc{};         // device list + per-sub-cube starts and lengths
     int64_t n_blocks = 0;
     int coils_per_pass = 8;
+    int use_tma = 1;            // bulk tensor copies for interior gather tiles
     int threads = 256;
     double taps = 0;
     float *U = nullptr;         // deapodization [N1 N2 N3]
@@ -335,6 +336,7 @@ int run_inverse(nufft3d_plan *p, const float2 *raw, float2 *x, int nc, int maxit
 
 size_t smem_interp_bytes(const Geom &g, int cb);
 size_t cand_smem_bytes(int n);
+int interp_check_error();  // reads and clears the interpolation timeout flag
 size_t smem_plane_bytes(int R, int cb);
 
 // Stage timing scope: records an event pair on stream s when profiling is on

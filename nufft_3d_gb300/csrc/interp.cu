@@ -16,7 +16,12 @@
 // computed in double at plan time and packed = lx | ly<<8 | lz<<16 the
 // sample's rounded position inside the padded tile.
 // Grid layout [K3][K2][K1][nc]; sorted sample data layout [nnz][nc].
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
+
+#include <cstring>
+#include <mutex>
 
 #include "internal.h"
 
@@ -231,6 +236,61 @@ __device__ __forceinline__ int eval_chunk(int base, const SampleGeo &sg, const C
 
 // Gather: tile staged coil-major ([CB][P^3] complex) -> ks.  kGroup lanes per
 // sample walk the candidate list; partial sums are reduced across the group.
+// ------------------------------------------------- TMA tile staging
+// Interior tiles of the gather (padded tile inside the grid on every axis)
+// are staged by one bulk tensor copy: the grid [K3][K2][K1][nc] complex is
+// described as a 5-D tensor (4 floats = one coil pair, x, y, z, coil pair)
+// whose last dimension has a 16-byte stride, so the box lands in shared
+// memory as the coil-pair planes [pair][z][y][x] the kernels read.  Tiles
+// that wrap around the grid edge use per-element asynchronous copies.
+// Waits are bounded: on expiry g_interp_err is set and the block returns.
+__device__ unsigned g_interp_err;
+
+__device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(unsigned bar, unsigned bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ void tma_load_5d(unsigned dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            int c4, unsigned bar)
+{
+    asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+                 : "memory");
+}
+
+// Bounded wait for phase 0 of the barrier; false if it expired.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar)
+{
+    for (int i = 0; i < (1 << 22); ++i)
+        if (mbar_try_wait(bar, 0)) return true;
+    return false;
+}
+
+__device__ __forceinline__ float2 *align128(float4 *p)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(p);
+    return reinterpret_cast<float2 *>(reinterpret_cast<char *>(p) + ((128u - (sa & 127u)) & 127u));
+}
+
 // acc[c] += w * tile(c, off): coil pairs come from one 16-byte load of a pair
 // plane; a quarter-warp is one sample's chunk of 8 candidates, whose tile
 // words the plan-time candidate order spreads over distinct bank groups.
@@ -260,18 +320,30 @@ template <int CB, bool RADIAL, int R>
 __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
                                             const float4 *__restrict__ samples, const int4 bi, const Geom &g,
                                             const KBParams &kb, float scale, const float *__restrict__ wsample,
-                                            const Cand &cd, float4 *smem4)
+                                            const Cand &cd, float4 *smem4, const CUtensorMap *tmap,
+                                            unsigned long long *bar)
 {
     constexpr int pv = Plane<R>::PS;
-    const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
+    const int Px = g.P[0];
     CandSmem cs;
-    float2 *tile = reinterpret_cast<float2 *>(carve_cand(cd, cs, smem4));
+    float2 *tile = align128(carve_cand(cd, cs, smem4));
     const int tid = bi.x;
     const int tx = tid % g.nt[0];
     const int ty = (tid / g.nt[0]) % g.nt[1];
     const int tz = tid / (g.nt[0] * g.nt[1]);
     const int ox = tx * g.T[0] - g.Ra[0], oy = ty * g.T[1] - g.Ra[1], oz = tz * g.T[2] - g.Ra[2];
     const int cb = min(CB, nc - c0);
+    const bool bulk = tmap != nullptr && ox >= 0 && oy >= 0 && oz >= 0 && ox + g.P[0] <= g.K[0] &&
+                      oy + g.P[1] <= g.K[1] && oz + g.P[2] <= g.K[2];
+    const unsigned bar_sa = bar ? (unsigned)__cvta_generic_to_shared(bar) : 0u;
+    if (bulk) {
+        if (threadIdx.x == 0) mbar_init(bar_sa, 1);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(bar_sa, (unsigned)(pv * (CB / 2) * sizeof(float4)));
+            tma_load_5d((unsigned)__cvta_generic_to_shared(tile), tmap, 0, ox, oy, oz, c0 / 2, bar_sa);
+        }
+    } else
     // stage the padded tile with asynchronous copies (no register round trip)
     for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int c, size_t gidx) {
         // coil pairs in float4 planes: coil c of point pt at float2 (c/2)*2*pv + 2*pt + (c&1)
@@ -286,7 +358,18 @@ __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2
     asm volatile("cp.async.commit_group;" ::: "memory");
     build_cand(cd, cs);
     asm volatile("cp.async.wait_all;" ::: "memory");
-    __syncthreads();
+    if (bulk) {
+        const bool done = mbar_wait_bounded(bar_sa);
+        if (__syncthreads_or(!done)) {     // block-uniform exit on expiry
+            if (threadIdx.x == 0) {
+                atomicOr(&g_interp_err, 1u);
+                mbar_wait_bounded(bar_sa);  // let the copy land before the block exits
+            }
+            return;
+        }
+    } else {
+        __syncthreads();
+    }
     const int lane = threadIdx.x & 31;
     const int lig = lane & (kGroup - 1);
     const unsigned gmask = 0xFFu << (lane & ~(kGroup - 1));
@@ -331,10 +414,13 @@ template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
 k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
          const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
-         KBParams kb, float scale, const float *__restrict__ wsample, Cand cd)
+         KBParams kb, float scale, const float *__restrict__ wsample, Cand cd,
+         const __grid_constant__ CUtensorMap tmap, int use_tma)
 {
     extern __shared__ float4 smem4[];
-    gather_body<CB, RADIAL, R>(G, ks, nc, c0, samples, blocks[blockIdx.x], g, kb, scale, wsample, cd, smem4);
+    __shared__ unsigned long long bar;
+    gather_body<CB, RADIAL, R>(G, ks, nc, c0, samples, blocks[blockIdx.x], g, kb, scale, wsample, cd, smem4,
+                               use_tma ? &tmap : nullptr, &bar);
 }
 
 // Spread: ks -> tile -> grid.  The tile accumulates in 32-bit fixed point
@@ -573,7 +659,7 @@ k_gather_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ ta
     const BatchInterp &b = vols[e.x];
     const Cand &cd = b.cand;
     gather_body<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, b.kb, b.scale, b.wsample,
-                               cd, smem4);
+                               cd, smem4, nullptr, nullptr);
 }
 
 template <int CB, bool RADIAL, int R>
@@ -639,13 +725,64 @@ size_t smem_plane_bytes(int R, int cb)
     return (size_t)ps * cb * sizeof(float2);
 }
 
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static std::once_flag once;
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+        else
+            cudaGetLastError();
+    });
+    return fn;
+}
+
+// The 5-D map of the grid for the gather's bulk tile copies (coil-pair box of
+// CB/2 pairs); false where it does not apply (odd nc, single coils, 2-D
+// tiles whose plane stride differs from the box) or the driver refuses it.
+template <int CB, int R>
+static bool gather_tensor_map(const nufft3d_plan *p, const float2 *G, int nc, CUtensorMap *m)
+{
+    const Geom &g = p->geom;
+    if (CB < 2 || nc % 2 || g.is2d || Plane<R>::PS != g.P[0] * g.P[1] * g.P[2]) return false;
+    auto enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint64_t row = (cuuint64_t)nc * sizeof(float2);
+    cuuint64_t dim[5] = {4, (cuuint64_t)g.K[0], (cuuint64_t)g.K[1], (cuuint64_t)g.K[2], (cuuint64_t)nc / 2};
+    cuuint64_t str[4] = {row, row * g.K[0], row * g.K[0] * g.K[1], sizeof(float4)};
+    cuuint32_t box[5] = {4, (cuuint32_t)g.P[0], (cuuint32_t)g.P[1], (cuuint32_t)g.P[2], CB / 2};
+    cuuint32_t es[5] = {1, 1, 1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, const_cast<float2 *>(G), dim, str, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+int interp_check_error()
+{
+    unsigned v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_interp_err, sizeof(v)) != cudaSuccess) return NUFFT3D_ERR_CUDA;
+    if (!v) return NUFFT3D_SUCCESS;
+    const unsigned zero = 0;
+    cudaMemcpyToSymbol(g_interp_err, &zero, sizeof(zero));
+    return fail(NUFFT3D_ERR_TIMEOUT, "a tile copy in the interpolation did not complete in time");
+}
+
 template <int CB, bool RADIAL, int R>
 static int gather_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, int c0, float scale,
                     const float *ws, cudaStream_t s)
 {
-    const size_t smem = smem_plane_bytes(R, CB) + cand_smem_bytes(p->n_cand);
+    // + 128: the tile is aligned to 128 bytes for the bulk copies
+    const size_t smem = smem_plane_bytes(R, CB) + cand_smem_bytes(p->n_cand) + 128;
+    alignas(64) CUtensorMap m;
+    std::memset(&m, 0, sizeof(m));
+    const int use_tma = p->use_tma && gather_tensor_map<CB, R>(p, G, nc, &m) ? 1 : 0;
     k_gather<CB, RADIAL, R><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
-        G, ks, nc, c0, p->samples, p->blocks, p->geom, p->kb, scale, ws, cand_of(p));
+        G, ks, nc, c0, p->samples, p->blocks, p->geom, p->kb, scale, ws, cand_of(p), m, use_tma);
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }

@@ -547,5 +547,6 @@ extern "C" int nufft3d_inverse_host(nufft3d_plan *p, const float *raw, float *x,
     NUFFT_TRY(run_inverse(p, (const float2 *)base, (float2 *)h.out, nc, maxit, damp, Wd, solver, tol, iters_host, s));
     NUFFT_CUDA_TRY(cudaMemcpyAsync(x, h.out, bx, cudaMemcpyDeviceToHost, s));
     NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    NUFFT_TRY(interp_check_error());
     return NUFFT3D_SUCCESS;
 }
