@@ -1,12 +1,13 @@
 // Host-side ordering of the candidate taps for shared-memory bank spread.
 //
 // The interpolation kernels read (gather) or add to (spread) the staged tile
-// at offsets base + off(candidate, octant).  In both, the 8 taps handled by
-// one instruction of a lane group -- a chunk of 8 consecutive candidates in
-// the gather, 8 consecutive entries of the compacted hit queue in the spread --
-// are conflict-free exactly when their tile offsets differ modulo 8 (the
-// 16-byte coil-pair words of the gather tile: 8 per 128-byte wavefront; the
-// spread's integer planes are shifted by 8 banks per coil pair).  The
+// at offsets base + off(candidate, octant).  In the gather a chunk of 8
+// consecutive candidates is read by 8 lanes in rotated coil-pair order (lanes
+// l and l+4 share the rotation), which is conflict-free when those two taps
+// have tile offsets of different parity.  In the spread 8 consecutive entries
+// of the compacted hit queue are added by one instruction, conflict-free when
+// their offsets differ modulo 8 (the integer planes are shifted by 8 banks per
+// coil pair).  The
 // distance-sorted candidate list is therefore re-partitioned by a seeded local
 // search: swaps between nearby chunks (keeping the near-to-far order that
 // lets whole chunks of far taps go idle) are kept by simulated annealing on
@@ -65,17 +66,21 @@ inline void bank_order(std::vector<int> &code, int Px, int PxPy, double J, int r
     std::vector<int> pos(n);  // position -> candidate
     for (int i = 0; i < n; ++i) pos[i] = i;
     const int nchunk = (n + 7) / 8, nblock = (n + 31) / 32;
+    // gather: lanes l and l+4 of a chunk read the same rotated coil pair of
+    // their taps, so a load takes a second wavefront when two such taps are
+    // both hit and have tile offsets of equal parity
     auto chunk_cost = [&](int c) {
         long t = 0;
-        const int b = 8 * c, e = b + 8 < n ? b + 8 : n;
+        const int b = 8 * c;
         for (int s = 0; s < S; ++s) {
             const uint8_t *sl = &slot[(size_t)s * n];
-            int cnt[9] = {0}, mx = 0;
-            for (int p = b; p < e; ++p) {
-                const int k = sl[pos[p]];
-                if (k < 8 && ++cnt[k] > mx) mx = cnt[k];
+            bool any = false, coll = false;
+            for (int l = 0; l < 8 && b + l < n; ++l) any |= sl[pos[b + l]] < 8;
+            for (int l = 0; l < 4 && b + l + 4 < n; ++l) {
+                const int u = sl[pos[b + l]], v = sl[pos[b + l + 4]];
+                coll |= u < 8 && v < 8 && ((u ^ v) & 1) == 0;
             }
-            t += mx;
+            t += any ? 1 + (coll ? 1 : 0) : 0;
         }
         return t;
     };

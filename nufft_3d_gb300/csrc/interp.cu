@@ -238,11 +238,10 @@ __device__ __forceinline__ int eval_chunk(int base, const SampleGeo &sg, const C
 // sample walk the candidate list; partial sums are reduced across the group.
 // ------------------------------------------------- TMA tile staging
 // Interior tiles of the gather (padded tile inside the grid on every axis)
-// are staged by one bulk tensor copy: the grid [K3][K2][K1][nc] complex is
-// described as a 5-D tensor (4 floats = one coil pair, x, y, z, coil pair)
-// whose last dimension has a 16-byte stride, so the box lands in shared
-// memory as the coil-pair planes [pair][z][y][x] the kernels read.  Tiles
-// that wrap around the grid edge use per-element asynchronous copies.
+// are staged by one bulk tensor copy of the box [z][y][x][CB coils] of the
+// grid [K3][K2][K1][nc] complex (4-D map: 2*nc floats, K1, K2, K3), which
+// lands point-major in shared memory.  Tiles that wrap around the grid edge
+// use per-element asynchronous copies into the same layout.
 // Waits are bounded: on expiry g_interp_err is set and the block returns.
 __device__ unsigned g_interp_err;
 
@@ -268,12 +267,12 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
     return ok != 0;
 }
 
-__device__ __forceinline__ void tma_load_5d(unsigned dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
-                                            int c4, unsigned bar)
+__device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map, int c0, int c1, int c2, int c3,
+                                            unsigned bar)
 {
-    asm volatile("cp.async.bulk.tensor.5d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-                 " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(dst),
-                 "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(c4), "r"(bar)
+    asm volatile("cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+                 " [%0], [%1, {%2, %3, %4, %5}], [%6];" ::"r"(dst),
+                 "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(bar)
                  : "memory");
 }
 
@@ -294,25 +293,54 @@ __device__ __forceinline__ float2 *align128(float4 *p)
 // acc[c] += w * tile(c, off): coil pairs come from one 16-byte load of a pair
 // plane; a quarter-warp is one sample's chunk of 8 candidates, whose tile
 // words the plan-time candidate order spreads over distinct bank groups.
-// acc[c] += w * tile(c, off): coil pairs come from one 16-byte load of a pair
-// plane.
-template <int CB, int PV>
-__device__ __forceinline__ void accumulate(float2 (&acc)[CB], const float2 *tile, int off, float w)
+// Gather tile layout: point-major, one record of CB coils (8*CB bytes) per
+// tile point, as the bulk tensor copy lands it.  Lane l of a sample's group
+// reads the 16-byte coil pairs of a tap in the rotated order pair = rot ^ k
+// (rot = l mod NP, k = 0..NP-1), so that in each load the 8 lanes touch 8
+// different 16-byte bank groups when lanes l and l+4 (same rot) hold taps of
+// different parity (the candidate order is chosen for that); acc holds the
+// pairs in that rotated order until unrotate().
+template <int CB>
+__device__ __forceinline__ void accumulate(float2 (&acc)[CB], const float2 *tile, int off, float w,
+                                           const int (&ko)[CB >= 2 ? CB / 2 : 1])
 {
-    if (CB >= 2) {
-        const float4 *t4 = reinterpret_cast<const float4 *>(tile);
+    if constexpr (CB >= 2) {
+        const char *pb = reinterpret_cast<const char *>(tile) + (size_t)off * (CB * 8);
 #pragma unroll
-        for (int q = 0; q < CB / 2; ++q) {
-            const float4 v = t4[(size_t)q * PV + off];
-            acc[2 * q].x = fmaf(w, v.x, acc[2 * q].x);
-            acc[2 * q].y = fmaf(w, v.y, acc[2 * q].y);
-            acc[2 * q + 1].x = fmaf(w, v.z, acc[2 * q + 1].x);
-            acc[2 * q + 1].y = fmaf(w, v.w, acc[2 * q + 1].y);
+        for (int k = 0; k < CB / 2; ++k) {
+            const float4 v = *reinterpret_cast<const float4 *>(pb + ko[k]);
+            acc[2 * k].x = fmaf(w, v.x, acc[2 * k].x);
+            acc[2 * k].y = fmaf(w, v.y, acc[2 * k].y);
+            acc[2 * k + 1].x = fmaf(w, v.z, acc[2 * k + 1].x);
+            acc[2 * k + 1].y = fmaf(w, v.w, acc[2 * k + 1].y);
         }
     } else {
         const float2 v = tile[off];
         acc[0].x = fmaf(w, v.x, acc[0].x);
         acc[0].y = fmaf(w, v.y, acc[0].y);
+    }
+}
+
+// acc[2k..2k+1] (pair rot ^ k) -> acc[2p..2p+1] (pair p): conditional swaps
+// of pair k with k^1 (rot bit 0) and k^2 (rot bit 1).
+template <int CB>
+__device__ __forceinline__ void unrotate(float2 (&acc)[CB], int rot)
+{
+    if constexpr (CB >= 4) {
+#pragma unroll
+        for (int b = 1; b < CB / 2; b <<= 1) {
+            const bool sw = rot & b;
+#pragma unroll
+            for (int k = 0; k < CB / 2; ++k) {
+                if (k & b) continue;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const float2 lo = acc[2 * k + h], hi = acc[2 * (k ^ b) + h];
+                    acc[2 * k + h] = sw ? hi : lo;
+                    acc[2 * (k ^ b) + h] = sw ? lo : hi;
+                }
+            }
+        }
     }
 }
 
@@ -323,7 +351,6 @@ __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2
                                             const Cand &cd, float4 *smem4, const CUtensorMap *tmap,
                                             unsigned long long *bar)
 {
-    constexpr int pv = Plane<R>::PS;
     const int Px = g.P[0];
     CandSmem cs;
     float2 *tile = align128(carve_cand(cd, cs, smem4));
@@ -340,14 +367,13 @@ __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2
         if (threadIdx.x == 0) mbar_init(bar_sa, 1);
         __syncthreads();
         if (threadIdx.x == 0) {
-            mbar_expect_tx(bar_sa, (unsigned)(pv * (CB / 2) * sizeof(float4)));
-            tma_load_5d((unsigned)__cvta_generic_to_shared(tile), tmap, 0, ox, oy, oz, c0 / 2, bar_sa);
+            mbar_expect_tx(bar_sa, (unsigned)(g.P[0] * g.P[1] * g.P[2] * CB * sizeof(float2)));
+            tma_load_4d((unsigned)__cvta_generic_to_shared(tile), tmap, 2 * c0, ox, oy, oz, bar_sa);
         }
     } else
     // stage the padded tile with asynchronous copies (no register round trip)
     for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int c, size_t gidx) {
-        // coil pairs in float4 planes: coil c of point pt at float2 (c/2)*2*pv + 2*pt + (c&1)
-        float2 *dst = CB >= 2 ? &tile[(size_t)(c >> 1) * 2 * pv + 2 * pt + (c & 1)] : &tile[pt];
+        float2 *dst = &tile[(size_t)pt * CB + c];
         if (c < cb) {
             const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
             asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(&G[gidx * nc + c0 + c]) : "memory");
@@ -373,6 +399,10 @@ __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2
     const int lane = threadIdx.x & 31;
     const int lig = lane & (kGroup - 1);
     const unsigned gmask = 0xFFu << (lane & ~(kGroup - 1));
+    const int rot = CB >= 2 ? lig & (CB / 2 - 1) : 0;
+    int ko[CB >= 2 ? CB / 2 : 1];
+#pragma unroll
+    for (int k = 0; k < (CB >= 2 ? CB / 2 : 1); ++k) ko[k] = (rot ^ k) << 4;
     const int grp = threadIdx.x / kGroup, ngrp = blockDim.x / kGroup;
     const int send = bi.y + bi.z;
     float4 rec_next = bi.y + grp < send ? __ldg(&samples[bi.y + grp]) : make_float4(0.f, 0.f, 0.f, 0.f);
@@ -391,9 +421,10 @@ __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2
             // (branchy form: a branch-free variant with predicated loads was slower here)
             const bool h0 = ci0 < sg.ln && tap<RADIAL>(ci0, sg, cs, kb, w0, off0);
             const bool h1 = ci1 < sg.ln && tap<RADIAL>(ci1, sg, cs, kb, w1, off1);
-            if (h0) accumulate<CB, pv>(acc, tile, off0, w0);
-            if (h1) accumulate<CB, pv>(acc, tile, off1, w1);
+            if (h0) accumulate<CB>(acc, tile, off0, w0, ko);
+            if (h1) accumulate<CB>(acc, tile, off1, w1, ko);
         }
+        unrotate<CB>(acc, rot);
 #pragma unroll
         for (int c = 0; c < CB; ++c) {
 #pragma unroll
@@ -742,22 +773,23 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
     return fn;
 }
 
-// The 5-D map of the grid for the gather's bulk tile copies (coil-pair box of
-// CB/2 pairs); false where it does not apply (odd nc, single coils, 2-D
-// tiles whose plane stride differs from the box) or the driver refuses it.
-template <int CB, int R>
+// The 4-D map of the grid for the gather's bulk tile copies (box of CB
+// coils per point); false where it does not apply (odd nc: row strides must
+// be multiples of 16 bytes; single coils: the box row must be 16 bytes or
+// more) or the driver refuses it.
+template <int CB>
 static bool gather_tensor_map(const nufft3d_plan *p, const float2 *G, int nc, CUtensorMap *m)
 {
     const Geom &g = p->geom;
-    if (CB < 2 || nc % 2 || g.is2d || Plane<R>::PS != g.P[0] * g.P[1] * g.P[2]) return false;
+    if (CB < 2 || nc % 2) return false;
     auto enc = tensor_map_encoder();
     if (!enc) return false;
     const cuuint64_t row = (cuuint64_t)nc * sizeof(float2);
-    cuuint64_t dim[5] = {4, (cuuint64_t)g.K[0], (cuuint64_t)g.K[1], (cuuint64_t)g.K[2], (cuuint64_t)nc / 2};
-    cuuint64_t str[4] = {row, row * g.K[0], row * g.K[0] * g.K[1], sizeof(float4)};
-    cuuint32_t box[5] = {4, (cuuint32_t)g.P[0], (cuuint32_t)g.P[1], (cuuint32_t)g.P[2], CB / 2};
-    cuuint32_t es[5] = {1, 1, 1, 1, 1};
-    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 5, const_cast<float2 *>(G), dim, str, box, es,
+    cuuint64_t dim[4] = {(cuuint64_t)2 * nc, (cuuint64_t)g.K[0], (cuuint64_t)g.K[1], (cuuint64_t)g.K[2]};
+    cuuint64_t str[3] = {row, row * g.K[0], row * g.K[0] * g.K[1]};
+    cuuint32_t box[4] = {2 * CB, (cuuint32_t)g.P[0], (cuuint32_t)g.P[1], (cuuint32_t)g.P[2]};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float2 *>(G), dim, str, box, es,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
@@ -780,7 +812,7 @@ static int gather_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, int c0
     const size_t smem = smem_plane_bytes(R, CB) + cand_smem_bytes(p->n_cand) + 128;
     alignas(64) CUtensorMap m;
     std::memset(&m, 0, sizeof(m));
-    const int use_tma = p->use_tma && gather_tensor_map<CB, R>(p, G, nc, &m) ? 1 : 0;
+    const int use_tma = p->use_tma && gather_tensor_map<CB>(p, G, nc, &m) ? 1 : 0;
     k_gather<CB, RADIAL, R><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
         G, ks, nc, c0, p->samples, p->blocks, p->geom, p->kb, scale, ws, cand_of(p), m, use_tma);
     NUFFT_CUDA_TRY(cudaGetLastError());
