@@ -164,6 +164,31 @@ int nufft3d_inverse_host(nufft3d_plan *plan, const float *raw_host, float *x_hos
                          int maxit, double damp, const float *W_host, int solver,
                          double tol, int *iters_host);
 
+/* The same solve started from x0 instead of 0 -- minres(A, b, tol, maxit,
+ * [], [], x0) as discrep.m:55-58 calls it, warm-starting each damp update
+ * from the previous image.  x holds x0 on entry and the image on return; the
+ * stop test stays relative to |A'W raw| as in MATLAB minres/pcg with x0.
+ * maxit = 0 is regridding (x0 ignored), as in nufft3d_inverse. */
+int nufft3d_inverse_x0(nufft3d_plan *plan, const float *raw_dev, float *x_dev, int nc,
+                       int maxit, double damp, const float *W_dev, int solver, double tol,
+                       int *iters_host, void *stream);
+/* im = obj.iNUFT(raw, maxit, damp, W, 'phase-constraint', lambda) --
+ * iNUFT.m:140-168 with pprojection (nufft_3d.m:325-334): after the MINRES
+ * solve, P = exp(i angle(convn(x, ones(3), 'same'))) (a 3x3 box in x-y per
+ * slice), then (P'A'WAP + damp^2 I + i lambda^2 imag) y = P'A'W raw is solved
+ * from 0 and im = P y.  The reference's solver pcgpc is external; this is CG
+ * with real inner products (FP64 scalars, stop |r| <= tol |b|).  maxit <= 1
+ * returns the plain result (iNUFT.m:77-78).  iters_host receives the
+ * constrained solve's iteration counts. */
+int nufft3d_inverse_phase(nufft3d_plan *plan, const float *raw_dev, float *x_dev, int nc, int maxit,
+                          double damp, double lambda, const float *W_dev, double tol, int *iters_host,
+                          void *stream);
+int nufft3d_inverse_phase_host(nufft3d_plan *plan, const float *raw_host, float *x_host, int nc, int maxit,
+                               double damp, double lambda, const float *W_host, double tol, int *iters_host);
+int nufft3d_inverse_x0_host(nufft3d_plan *plan, const float *raw_host, float *x_host, int nc,
+                            int maxit, double damp, const float *W_host, int solver,
+                            double tol, int *iters_host);
+
 /* ---- Batches: many volumes (different N, trajectories, coil counts) per launch.
  * No single counterpart in the reference, which handles one object at a time;
  * each volume's result equals what fNUFT / aNUFT / iNUFT of its own plan

@@ -73,6 +73,14 @@ SIGNATURES = {
                                        ctypes.c_int, ctypes.c_double, _P, _P]),
     "nufft3d_inverse_host": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_double, _P,
                                             ctypes.c_int, ctypes.c_double, _P]),
+    "nufft3d_inverse_phase": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                             ctypes.c_double, _P, ctypes.c_double, _P, _P]),
+    "nufft3d_inverse_phase_host": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                  ctypes.c_double, _P, ctypes.c_double, _P]),
+    "nufft3d_inverse_x0": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_double, _P,
+                                          ctypes.c_int, ctypes.c_double, _P, _P]),
+    "nufft3d_inverse_x0_host": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_int, ctypes.c_double, _P,
+                                               ctypes.c_int, ctypes.c_double, _P]),
     "nufft3d_density": (ctypes.c_int, [_P, ctypes.c_int]),
     "nufft3d_batch_create": (ctypes.c_int, [_P, _P, ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
     "nufft3d_batch_destroy": (ctypes.c_int, [_P]),

@@ -236,6 +236,7 @@ struct SolverWork {
     float2 *x = nullptr, *r = nullptr, *p = nullptr, *q = nullptr, *v = nullptr,
            *vprev = nullptr, *w1 = nullptr, *w2 = nullptr;
     double *partial = nullptr;  // [nc * nchunk]
+    double *bpart = nullptr;    // [nc * nchunk] |b|^2 partial sums of a warm start
     double *scal = nullptr;     // per-coil scalar state
     int *iters = nullptr;       // per-coil iteration counts
     int nchunk = 0;
@@ -332,7 +333,7 @@ int run_density(nufft3d_plan *p, int maxit, cudaStream_t s);
 int ensure_solver(nufft3d_plan *p, int nc);
 int run_inverse(nufft3d_plan *p, const float2 *raw, float2 *x, int nc, int maxit,
                 double damp, const float *W_orig, int solver, double tol, int *iters_host,
-                cudaStream_t s);
+                cudaStream_t s, bool warm = false);
 
 size_t smem_interp_bytes(const Geom &g, int cb);
 size_t cand_smem_bytes(int n);

@@ -528,7 +528,10 @@ __device__ __forceinline__ void spread_body(const float2 *__restrict__ ks, float
             m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
         }
     }
-    for (int t = threadIdx.x; t < ps * CB * 2; t += blockDim.x) tile[t] = 0;
+    {   // zero the integer planes with 16-byte stores (ps * CB * 2 is a multiple of 4)
+        int4 *t4 = reinterpret_cast<int4 *>(tile);
+        for (int t = threadIdx.x; t < ps * CB / 2; t += blockDim.x) t4[t] = make_int4(0, 0, 0, 0);
+    }
     build_cand(cd, cs);
     const float ymax = block_max(m, red);   // contains __syncthreads
     if (!(ymax > 0.f)) return;             // nothing to add (block-uniform)

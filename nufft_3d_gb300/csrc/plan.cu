@@ -446,7 +446,7 @@ static void free_plan_memory(nufft3d_plan *p)
     F(p->stage.out);
     SolverWork &w = p->solver;
     F(w.x); F(w.r); F(w.p); F(w.q); F(w.v); F(w.vprev); F(w.w1); F(w.w2);
-    F(w.partial); F(w.scal); F(w.iters);
+    F(w.partial); F(w.bpart); F(w.scal); F(w.iters);
     profile_release(p);
     if (p->own_stream) cudaStreamDestroy(p->own_stream);
     p->tables.reset();

@@ -296,6 +296,35 @@ k_mr_update(float2 *__restrict__ x, float2 *__restrict__ v, float2 *__restrict__
     }
 }
 
+// Warm start (x0 given): dst = b - A x0, in place over b.
+__global__ void __launch_bounds__(kVecThreads)
+k_sub_inplace(float2 *__restrict__ b, const float2 *__restrict__ ax, size_t n)
+{
+    const int c = blockIdx.y;
+    VEC_LOOP(i, n)
+    {
+        const float2 u = b[c * n + i], v = ax[c * n + i];
+        b[c * n + i] = make_float2(u.x - v.x, u.y - v.y);
+    }
+}
+
+// Warm start: stop tests stay relative to |b| (MATLAB minres/pcg with x0):
+// CG compares |r| with tol*|b| through S_BN2; MINRES compares its residual
+// estimate (which starts at |r0|) with tol*S_BETA1, so the tolerance is
+// rescaled by |b|/|r0|.
+__global__ void k_warm_ref(const double *__restrict__ part_b, double *__restrict__ scal, int nc, int minres)
+{
+    const int c = threadIdx.x;
+    if (c >= nc) return;
+    double *S = scal + c * kS;
+    const double b2 = sum_parts(part_b, c);
+    if (minres) {
+        if (S[S_BETA1] > 0) S[S_TOL] *= std::sqrt(b2) / S[S_BETA1];
+    } else {
+        S[S_BN2] = b2;
+    }
+}
+
 __global__ void k_weights(const float *__restrict__ W, const int32_t *__restrict__ perm,
                           const float *__restrict__ d, int64_t nnz, float *__restrict__ ws)
 {
@@ -307,6 +336,82 @@ __global__ void k_iters_out(const double *__restrict__ scal, int nc, int *__rest
 {
     const int c = threadIdx.x;
     if (c < nc) out[c] = (int)scal[c * kS + S_ITERS];
+}
+
+// ------------------------------------------------------ phase constraint
+// iNUFT.m:147-150: P = exp(i angle(convn(x, ones(3), 'same'))).  ones(3) is
+// a 3x3 matrix, so the box sum runs over x and y only, slice by slice, with
+// zeros outside the image; angle(0) = 0 gives P = 1.
+__global__ void k_box_phase(const float2 *__restrict__ x, float2 *__restrict__ P, int N1, int N2, size_t nimg)
+{
+    const int c = blockIdx.y;
+    const float2 *X = x + c * nimg;
+    VEC_LOOP(i, nimg)
+    {
+        const int ix = (int)(i % N1), iy = (int)((i / N1) % N2);
+        const size_t slice = i - (size_t)ix - (size_t)iy * N1;
+        float sr = 0.f, si = 0.f;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int yy = iy + dy;
+            if (yy < 0 || yy >= N2) continue;
+            for (int dx = -1; dx <= 1; ++dx) {
+                const int xx = ix + dx;
+                if (xx < 0 || xx >= N1) continue;
+                const float2 v = X[slice + (size_t)yy * N1 + xx];
+                sr += v.x;
+                si += v.y;
+            }
+        }
+        const float m = sqrtf(sr * sr + si * si);
+        P[c * nimg + i] = m > 0.f ? make_float2(sr / m, si / m) : make_float2(1.f, 0.f);
+    }
+}
+
+// y = P .* x (conj_p = 0) or conj(P) .* x (conj_p = 1), in place allowed
+__global__ void k_phase_mul(float2 *__restrict__ y, const float2 *__restrict__ x, const float2 *__restrict__ P,
+                            size_t n, int conj_p)
+{
+    const int c = blockIdx.y;
+    VEC_LOOP(i, n)
+    {
+        const float2 a = x[c * n + i], q = P[c * n + i];
+        const float qi = conj_p ? -q.y : q.y;
+        y[c * n + i] = make_float2(a.x * q.x - a.y * qi, a.x * qi + a.y * q.x);
+    }
+}
+
+// nufft_3d.m:333: y = conj(P) .* y + i lambda^2 imag(x)
+__global__ void k_phase_finish(float2 *__restrict__ y, const float2 *__restrict__ x, const float2 *__restrict__ P,
+                               size_t n, float lam2)
+{
+    const int c = blockIdx.y;
+    VEC_LOOP(i, n)
+    {
+        const float2 a = y[c * n + i], q = P[c * n + i];
+        const float xi = x[c * n + i].y;
+        y[c * n + i] = make_float2(a.x * q.x + a.y * q.y, a.y * q.x - a.x * q.y + lam2 * xi);
+    }
+}
+
+// The phase-constrained normal operator (pprojection, nufft_3d.m:325-334):
+// y = P' A'WA (P x) + damp^2 x + i lambda^2 imag(x), real-linear in x.
+struct PhaseOp {
+    const float2 *P;
+    float2 *tmp;
+    float lam2;
+};
+
+static int apply_normal(nufft3d_plan *p, const float2 *x, float2 *y, int nc, double damp, const float *ws,
+                        const PhaseOp *ph, cudaStream_t s)
+{
+    if (!ph) return op_normal(p, x, y, nc, damp, ws, s);
+    const size_t n = p->solver.nimg;
+    const dim3 grid(kChunks, nc);
+    k_phase_mul<<<grid, kVecThreads, 0, s>>>(ph->tmp, x, ph->P, n, 0);
+    NUFFT_TRY(op_normal(p, ph->tmp, y, nc, damp, ws, s));
+    k_phase_finish<<<grid, kVecThreads, 0, s>>>(y, x, ph->P, n, ph->lam2);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
 }
 
 // ---------------------------------------------------------------- host
@@ -342,11 +447,13 @@ int ensure_solver(nufft3d_plan *p, int nc)
             *pp = nullptr;
         }
     if (w.partial) cudaFree(w.partial);
+    if (w.bpart) cudaFree(w.bpart);
     if (w.scal) cudaFree(w.scal);
     if (w.iters) cudaFree(w.iters);
     w = SolverWork();
     for (auto pp : vecs) NUFFT_CUDA_TRY(cudaMalloc((void **)pp, nimg * nc * sizeof(float2)));
     NUFFT_CUDA_TRY(cudaMalloc(&w.partial, sizeof(double) * kChunks * nc));
+    NUFFT_CUDA_TRY(cudaMalloc(&w.bpart, sizeof(double) * kChunks * nc));
     NUFFT_CUDA_TRY(cudaMalloc(&w.scal, sizeof(double) * kS * nc));
     NUFFT_CUDA_TRY(cudaMalloc(&w.iters, sizeof(int) * nc));
     w.nc = nc;
@@ -355,12 +462,13 @@ int ensure_solver(nufft3d_plan *p, int nc)
     return NUFFT3D_SUCCESS;
 }
 
-static int cg_iteration(nufft3d_plan *p, float2 *x, int nc, double damp, const float *ws, cudaStream_t s)
+static int cg_iteration(nufft3d_plan *p, float2 *x, int nc, double damp, const float *ws, cudaStream_t s,
+                        const PhaseOp *ph = nullptr)
 {
     SolverWork &w = p->solver;
     const size_t n = w.nimg;
     const dim3 grid(kChunks, nc);
-    NUFFT_TRY(op_normal(p, w.p, w.q, nc, damp, ws, s));
+    NUFFT_TRY(apply_normal(p, w.p, w.q, nc, damp, ws, ph, s));
     k_dot<<<grid, kVecThreads, 0, s>>>(w.p, w.q, n, w.partial);
     k_cg_alpha<<<1, 32 * ((nc + 31) / 32), 0, s>>>(w.partial, w.scal, nc);
     k_cg_xr<<<grid, kVecThreads, 0, s>>>(x, w.r, w.p, w.q, n, w.scal, w.partial);
@@ -386,8 +494,36 @@ static int minres_iteration(nufft3d_plan *p, float2 *x, int nc, double damp, con
     return NUFFT3D_SUCCESS;
 }
 
+// Captures one solver iteration (the operator and the vector kernels) as a
+// CUDA graph and replays it maxit times on `own`.
+template <typename Body>
+static int replay_iterations(cudaStream_t own, int maxit, Body &&body)
+{
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int st;
+    cudaError_t ce;
+    {
+        NUFFT_DEVICE_LOCK;
+        NUFFT_CUDA_TRY(cudaStreamBeginCapture(own, cudaStreamCaptureModeThreadLocal));
+        st = body(own);
+        ce = cudaStreamEndCapture(own, &graph);
+        if (st == NUFFT3D_SUCCESS && ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+    }
+    if (st != NUFFT3D_SUCCESS) {
+        if (exec) cudaGraphExecDestroy(exec);
+        return st;
+    }
+    if (ce != cudaSuccess) return fail(NUFFT3D_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    for (int it = 0; it < maxit && ce == cudaSuccess; ++it) ce = cudaGraphLaunch(exec, own);
+    cudaGraphExecDestroy(exec);
+    if (ce != cudaSuccess) return fail(NUFFT3D_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(ce));
+    return NUFFT3D_SUCCESS;
+}
+
 int run_inverse(nufft3d_plan *p, const float2 *raw, float2 *x, int nc, int maxit, double damp,
-                const float *W_orig, int solver, double tol, int *iters_host, cudaStream_t s)
+                const float *W_orig, int solver, double tol, int *iters_host, cudaStream_t s, bool warm)
 {
     cudaStream_t own = p->own_stream;
     cudaEvent_t ev = nullptr;
@@ -414,51 +550,100 @@ int run_inverse(nufft3d_plan *p, const float2 *raw, float2 *x, int nc, int maxit
         const size_t vb = n * nc * sizeof(float2);
         const dim3 grid(kChunks, nc);
         const int th1 = 32 * ((nc + 31) / 32);
-        NUFFT_CUDA_TRY(cudaMemsetAsync(x, 0, vb, own));
+        if (!warm) NUFFT_CUDA_TRY(cudaMemsetAsync(x, 0, vb, own));
+        // right-hand side b = A'W raw (into r for CG, q for MINRES); with a
+        // warm start the partial sums of |b|^2 go to w.bpart and the Krylov
+        // start vector becomes b - A x0
+        float2 *bvec = solver == NUFFT3D_SOLVER_CG ? w.r : w.q;
+        NUFFT_TRY(op_adjoint_weighted(p, raw, bvec, nc, ws, own));
+        if (warm) {
+            k_dot<<<grid, kVecThreads, 0, own>>>(bvec, bvec, n, w.bpart);
+            NUFFT_TRY(op_normal(p, x, w.v, nc, damp, ws, own));         // A x0 (v is reset below)
+            k_sub_inplace<<<grid, kVecThreads, 0, own>>>(bvec, w.v, n);
+        }
         if (solver == NUFFT3D_SOLVER_CG) {
-            NUFFT_TRY(op_adjoint_weighted(p, raw, w.r, nc, ws, own)); // b = A'W raw
             NUFFT_CUDA_TRY(cudaMemcpyAsync(w.p, w.r, vb, cudaMemcpyDeviceToDevice, own));
             k_dot<<<grid, kVecThreads, 0, own>>>(w.r, w.r, n, w.partial);
             k_cg_init<<<1, th1, 0, own>>>(w.partial, w.scal, nc, tol);
+            if (warm) k_warm_ref<<<1, th1, 0, own>>>(w.bpart, w.scal, nc, 0);
         } else {
-            NUFFT_TRY(op_adjoint_weighted(p, raw, w.q, nc, ws, own)); // b
             k_dot<<<grid, kVecThreads, 0, own>>>(w.q, w.q, n, w.partial);
             k_mr_init<<<1, th1, 0, own>>>(w.partial, w.scal, nc, tol);
+            if (warm) k_warm_ref<<<1, th1, 0, own>>>(w.bpart, w.scal, nc, 1);
             k_copy_scaled<<<grid, kVecThreads, 0, own>>>(w.v, w.q, n, w.scal, S_BETA1);
             NUFFT_CUDA_TRY(cudaMemsetAsync(w.vprev, 0, vb, own));
             NUFFT_CUDA_TRY(cudaMemsetAsync(w.w1, 0, vb, own));
             NUFFT_CUDA_TRY(cudaMemsetAsync(w.w2, 0, vb, own));
         }
         NUFFT_CUDA_TRY(cudaGetLastError());
-        // capture one iteration and replay it maxit times
-        cudaGraph_t graph = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        int st;
-        cudaError_t ce;
-        {
-            NUFFT_DEVICE_LOCK;
-            NUFFT_CUDA_TRY(cudaStreamBeginCapture(own, cudaStreamCaptureModeThreadLocal));
-            st = solver == NUFFT3D_SOLVER_CG ? cg_iteration(p, x, nc, damp, ws, own)
-                                             : minres_iteration(p, x, nc, damp, ws, own);
-            ce = cudaStreamEndCapture(own, &graph);
-            if (st == NUFFT3D_SUCCESS && ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
-            if (graph) cudaGraphDestroy(graph);
-        }
-        if (st != NUFFT3D_SUCCESS) {
-            if (exec) cudaGraphExecDestroy(exec);
-            return st;
-        }
-        if (ce != cudaSuccess) return fail(NUFFT3D_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
-        if (ce != cudaSuccess) return fail(NUFFT3D_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
-        for (int it = 0; it < maxit && ce == cudaSuccess; ++it) ce = cudaGraphLaunch(exec, own);
-        cudaGraphExecDestroy(exec);
-        if (ce != cudaSuccess) return fail(NUFFT3D_ERR_CUDA, std::string("graph launch: ") + cudaGetErrorString(ce));
+        NUFFT_TRY(replay_iterations(own, maxit, [&](cudaStream_t cs) {
+            return solver == NUFFT3D_SOLVER_CG ? cg_iteration(p, x, nc, damp, ws, cs)
+                                               : minres_iteration(p, x, nc, damp, ws, cs);
+        }));
         if (iters_host) {
             k_iters_out<<<1, th1, 0, own>>>(w.scal, nc, w.iters);
             NUFFT_CUDA_TRY(cudaGetLastError());
             NUFFT_CUDA_TRY(cudaMemcpyAsync(iters_host, w.iters, sizeof(int) * nc, cudaMemcpyDeviceToHost, own));
             NUFFT_CUDA_TRY(cudaStreamSynchronize(own));
         }
+    }
+    if (s != own) {
+        NUFFT_CUDA_TRY(cudaEventRecord(ev, own));
+        NUFFT_CUDA_TRY(cudaStreamWaitEvent(s, ev, 0));
+    }
+    return NUFFT3D_SUCCESS;
+}
+
+// iNUFT.m:140-168, 'phase-constraint': the MINRES image x gives the smooth
+// phase P; then (P'A'WAP + damp^2 + lambda^2 imag) y = P'A'W raw is solved
+// from y = 0 and the image is P y.  The reference's solver for this
+// real-linear system, pcgpc, lives in an external package; here it is
+// conjugate gradients with real inner products Re<a, b> (the operator is
+// self-adjoint and positive definite for that inner product), FP64 scalars,
+// stop on |r| <= tol |b|.
+int run_inverse_phase(nufft3d_plan *p, const float2 *raw, float2 *x, int nc, int maxit, double damp, double lambda,
+                      const float *W_orig, double tol, int *iters_host, cudaStream_t s)
+{
+    NUFFT_TRY(run_inverse(p, raw, x, nc, maxit, damp, W_orig, NUFFT3D_SOLVER_MINRES, tol, iters_host, s, false));
+    if (maxit <= 1) return NUFFT3D_SUCCESS;  // iNUFT.m:77-78: no effect with maxit <= 1
+    cudaStream_t own = p->own_stream;
+    cudaEvent_t ev = nullptr;
+    NUFFT_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    struct EvGuard {
+        cudaEvent_t e;
+        ~EvGuard() { cudaEventDestroy(e); }
+    } eg{ev};
+    if (s != own) {
+        NUFFT_CUDA_TRY(cudaEventRecord(ev, s));
+        NUFFT_CUDA_TRY(cudaStreamWaitEvent(own, ev, 0));
+    }
+    const float *ws = nullptr;
+    NUFFT_TRY(prepare_weights(p, W_orig, &ws, own));
+    NUFFT_TRY(ensure_solver(p, nc));
+    SolverWork &w = p->solver;
+    const size_t n = w.nimg;
+    const size_t vb = n * nc * sizeof(float2);
+    const dim3 grid(kChunks, nc);
+    const int th1 = 32 * ((nc + 31) / 32);
+    PhaseOp ph{w.w1, w.w2, (float)(lambda * lambda)};
+    k_box_phase<<<grid, kVecThreads, 0, own>>>(x, w.w1, p->N[0], p->N[1], n);
+    NUFFT_TRY(op_adjoint_weighted(p, raw, w.r, nc, ws, own));   // A'W raw
+    k_phase_mul<<<grid, kVecThreads, 0, own>>>(w.r, w.r, w.w1, n, 1);  // b = P' A'W raw
+    NUFFT_CUDA_TRY(cudaMemsetAsync(x, 0, vb, own));
+    NUFFT_CUDA_TRY(cudaMemcpyAsync(w.p, w.r, vb, cudaMemcpyDeviceToDevice, own));
+    k_dot<<<grid, kVecThreads, 0, own>>>(w.r, w.r, n, w.partial);
+    k_cg_init<<<1, th1, 0, own>>>(w.partial, w.scal, nc, tol);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    NUFFT_TRY(replay_iterations(own, maxit, [&](cudaStream_t cs) {
+        return cg_iteration(p, x, nc, damp, ws, cs, &ph);
+    }));
+    k_phase_mul<<<grid, kVecThreads, 0, own>>>(x, x, w.w1, n, 0);  // x = P y
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    if (iters_host) {
+        k_iters_out<<<1, th1, 0, own>>>(w.scal, nc, w.iters);
+        NUFFT_CUDA_TRY(cudaGetLastError());
+        NUFFT_CUDA_TRY(cudaMemcpyAsync(iters_host, w.iters, sizeof(int) * nc, cudaMemcpyDeviceToHost, own));
+        NUFFT_CUDA_TRY(cudaStreamSynchronize(own));
     }
     if (s != own) {
         NUFFT_CUDA_TRY(cudaEventRecord(ev, own));
@@ -505,11 +690,22 @@ extern "C" int nufft3d_inverse(nufft3d_plan *p, const float *raw, float *x, int 
     NUFFT_TRY(check_inverse(p, raw, x, nc, maxit, damp, solver));
     DevGuardS g(p->device);
     return run_inverse(p, (const float2 *)raw, (float2 *)x, nc, maxit, damp, W, solver, tol, iters_host,
-                       (cudaStream_t)stream);
+                       (cudaStream_t)stream, false);
 }
 
-extern "C" int nufft3d_inverse_host(nufft3d_plan *p, const float *raw, float *x, int nc, int maxit,
-                                    double damp, const float *W, int solver, double tol, int *iters_host)
+extern "C" int nufft3d_inverse_x0(nufft3d_plan *p, const float *raw, float *x, int nc, int maxit, double damp,
+                                  const float *W, int solver, double tol, int *iters_host, void *stream)
+{
+    clear_error();
+    NUFFT_TRY(check_inverse(p, raw, x, nc, maxit, damp, solver));
+    DevGuardS g(p->device);
+    return run_inverse(p, (const float2 *)raw, (float2 *)x, nc, maxit, damp, W, solver, tol, iters_host,
+                       (cudaStream_t)stream, maxit > 0);
+}
+
+// lambda >= 0 selects the phase-constrained solve (solver ignored)
+static int inverse_host(nufft3d_plan *p, const float *raw, float *x, int nc, int maxit, double damp,
+                        const float *W, int solver, double tol, int *iters_host, bool warm, double lambda = -1)
 {
     clear_error();
     NUFFT_TRY(check_inverse(p, raw, x, nc, maxit, damp, solver));
@@ -544,9 +740,48 @@ extern "C" int nufft3d_inverse_host(nufft3d_plan *p, const float *raw, float *x,
     float *Wd = W ? (float *)(base + ((braw + 255) / 256) * 256) : nullptr;
     NUFFT_CUDA_TRY(cudaMemcpyAsync(base, raw, braw, cudaMemcpyHostToDevice, s));
     if (W) NUFFT_CUDA_TRY(cudaMemcpyAsync(Wd, W, bW, cudaMemcpyHostToDevice, s));
-    NUFFT_TRY(run_inverse(p, (const float2 *)base, (float2 *)h.out, nc, maxit, damp, Wd, solver, tol, iters_host, s));
+    if (warm) NUFFT_CUDA_TRY(cudaMemcpyAsync(h.out, x, bx, cudaMemcpyHostToDevice, s));
+    if (lambda >= 0)
+        NUFFT_TRY(run_inverse_phase(p, (const float2 *)base, (float2 *)h.out, nc, maxit, damp, lambda, Wd, tol,
+                                    iters_host, s));
+    else
+        NUFFT_TRY(run_inverse(p, (const float2 *)base, (float2 *)h.out, nc, maxit, damp, Wd, solver, tol,
+                              iters_host, s, warm));
     NUFFT_CUDA_TRY(cudaMemcpyAsync(x, h.out, bx, cudaMemcpyDeviceToHost, s));
     NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
     NUFFT_TRY(interp_check_error());
     return NUFFT3D_SUCCESS;
+}
+
+extern "C" int nufft3d_inverse_host(nufft3d_plan *p, const float *raw, float *x, int nc, int maxit,
+                                    double damp, const float *W, int solver, double tol, int *iters_host)
+{
+    return inverse_host(p, raw, x, nc, maxit, damp, W, solver, tol, iters_host, false);
+}
+
+extern "C" int nufft3d_inverse_x0_host(nufft3d_plan *p, const float *raw, float *x, int nc, int maxit,
+                                       double damp, const float *W, int solver, double tol, int *iters_host)
+{
+    return inverse_host(p, raw, x, nc, maxit, damp, W, solver, tol, iters_host, maxit > 0);
+}
+
+extern "C" int nufft3d_inverse_phase(nufft3d_plan *p, const float *raw, float *x, int nc, int maxit, double damp,
+                                     double lambda, const float *W, double tol, int *iters_host, void *stream)
+{
+    clear_error();
+    NUFFT_TRY(check_inverse(p, raw, x, nc, maxit, damp, NUFFT3D_SOLVER_MINRES));
+    if (!std::isfinite(lambda) || lambda < 0) return fail(NUFFT3D_ERR_ARG, "lambda must be finite and nonnegative");
+    DevGuardS g(p->device);
+    return run_inverse_phase(p, (const float2 *)raw, (float2 *)x, nc, maxit, damp, lambda, W, tol, iters_host,
+                             (cudaStream_t)stream);
+}
+
+extern "C" int nufft3d_inverse_phase_host(nufft3d_plan *p, const float *raw, float *x, int nc, int maxit,
+                                          double damp, double lambda, const float *W, double tol, int *iters_host)
+{
+    if (!std::isfinite(lambda) || lambda < 0) {
+        clear_error();
+        return fail(NUFFT3D_ERR_ARG, "lambda must be finite and nonnegative");
+    }
+    return inverse_host(p, raw, x, nc, maxit, damp, W, NUFFT3D_SOLVER_MINRES, tol, iters_host, false, lambda);
 }

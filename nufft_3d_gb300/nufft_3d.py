@@ -295,19 +295,33 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
         return nc, nr, ny
 
     def iNUFT(self, raw, maxit=20, damp=0.0, W=None, constraint=None, lam=None, solver="minres",  # noqa: N802
-              tol=1e-4, return_iters=False):
+              tol=1e-4, return_iters=False, x0=None):
         """im = obj.iNUFT(raw, maxit, damp, W) -> (N1, N2, N3, nc) (iNUFT.m).
 
         Each coil is solved as its own system; ``solver`` 'minres' (the
         reference's) or 'cg'; ``tol=0`` runs exactly ``maxit`` iterations.
+        ``x0`` (same shape and kind as the result) starts the solve from an
+        earlier image instead of zero, as discrep.m:55-58 does.
         """
+        maxit = 20 if maxit is None else maxit
+        phase = False
         if constraint:
             if constraint not in ("phase-constraint", "compressed-sensing", "parallel-imaging-sake",
                                   "parallel-imaging-pruno"):
                 raise ValueError("unknown constraint")
-            raise NotImplementedError("constraint '%s' is not implemented (experimental in the reference, "
-                                      "needs the external 'parallel' package)" % constraint)
-        maxit = 20 if maxit is None else maxit
+            if constraint != "phase-constraint":
+                raise NotImplementedError("constraint '%s' is not implemented (experimental in the reference, "
+                                          "needs the external 'parallel' package)" % constraint)
+            if lam is None:
+                raise ValueError("lambda must be supplied with %s" % constraint)   # iNUFT.m:87-89
+            if not (np.isscalar(lam) and np.isfinite(lam) and lam >= 0):
+                raise ValueError("lambda must be a scalar finite nonnegative number")
+            if x0 is not None:
+                raise ValueError("x0 is not used with a constraint")
+            phase = maxit > 1
+            if not phase:
+                import warnings
+                warnings.warn("phase constraint is only effective when maxit>1")
         if not (np.isscalar(maxit) and np.isfinite(maxit) and maxit >= 0 and int(maxit) == maxit):
             raise ValueError("maxit must be a scalar nonnegative integer")
         damp = 0.0 if damp is None else damp
@@ -322,11 +336,22 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
             if W is not None and not np.isscalar(W) and (W.numel() if _is_torch(W) else np.size(W)) > 1:
                 Wn = W.detach().cpu().numpy() if _is_torch(W) else np.asarray(W)
                 Wt = torch.from_numpy(self._weights(Wn, None, None)).to(raw.device)
-            out = torch.empty((nc,) + tuple(int(v) for v in self.N[::-1]), dtype=torch.complex64, device=raw.device)
+            shape = (nc,) + tuple(int(v) for v in self.N[::-1])
+            if x0 is not None:
+                out = x0.detach().to(device=raw.device, dtype=torch.complex64).reshape(shape).contiguous().clone()
+                fn = self._L.nufft3d_inverse_x0
+            else:
+                out = torch.empty(shape, dtype=torch.complex64, device=raw.device)
+                fn = self._L.nufft3d_inverse
             its = (ctypes.c_int * nc)()
-            _lib.check(self._L.nufft3d_inverse(self.plan, raw.data_ptr(), out.data_ptr(), nc, int(maxit), float(damp),
-                                               Wt.data_ptr() if Wt is not None else None, sv, float(tol),
-                                               ctypes.cast(its, ctypes.c_void_p), self._stream_ptr(raw)))
+            wp = Wt.data_ptr() if Wt is not None else None
+            if phase:
+                _lib.check(self._L.nufft3d_inverse_phase(self.plan, raw.data_ptr(), out.data_ptr(), nc, int(maxit),
+                                                         float(damp), float(lam), wp, float(tol),
+                                                         ctypes.cast(its, ctypes.c_void_p), self._stream_ptr(raw)))
+            else:
+                _lib.check(fn(self.plan, raw.data_ptr(), out.data_ptr(), nc, int(maxit), float(damp), wp, sv,
+                              float(tol), ctypes.cast(its, ctypes.c_void_p), self._stream_ptr(raw)))
             self.last_iters = list(its)
             return (out, list(its)) if return_iters else out
         raw = np.asarray(raw)
@@ -336,16 +361,32 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
             warnings.warn("weighting is only effective when maxit>1")
         Wf = self._weights(W, nr, ny)
         rin = np.asfortranarray(raw.astype(np.complex64).reshape(self.M, nc, order="F"))
-        out = np.empty(tuple(self.N) + (nc,), dtype=np.complex64, order="F")
+        if x0 is not None:
+            out = np.array(np.asarray(x0, dtype=np.complex64).reshape(tuple(self.N) + (nc,), order="F"),
+                           dtype=np.complex64, order="F", copy=True)
+            fn = self._L.nufft3d_inverse_x0_host
+        else:
+            out = np.empty(tuple(self.N) + (nc,), dtype=np.complex64, order="F")
+            fn = self._L.nufft3d_inverse_host
         its = (ctypes.c_int * nc)()
-        _lib.check(self._L.nufft3d_inverse_host(self.plan, rin.ctypes.data, out.ctypes.data, nc, int(maxit),
-                                                float(damp), Wf.ctypes.data if Wf is not None else None, sv,
-                                                float(tol), ctypes.cast(its, ctypes.c_void_p)))
+        wp = Wf.ctypes.data if Wf is not None else None
+        if phase:
+            _lib.check(self._L.nufft3d_inverse_phase_host(self.plan, rin.ctypes.data, out.ctypes.data, nc,
+                                                          int(maxit), float(damp), float(lam), wp, float(tol),
+                                                          ctypes.cast(its, ctypes.c_void_p)))
+        else:
+            _lib.check(fn(self.plan, rin.ctypes.data, out.ctypes.data, nc, int(maxit), float(damp), wp, sv,
+                          float(tol), ctypes.cast(its, ctypes.c_void_p)))
         self.last_iters = list(its)
         return (out, list(its)) if return_iters else out
 
-    def discrep(self, data, stddev=None, iters=20, maxit=None, solver="minres"):
-        """Discrepancy-principle estimate of damp (discrep.m:2-69)."""
+    def discrep(self, data, stddev=None, iters=20, maxit=20, solver="minres"):
+        """Discrepancy-principle estimate of damp (discrep.m:2-69).
+
+        20 updates damp <- damp * discrepancy / |A x - data|, each solving
+        (A'DA + damp^2 I) x = A'D data by MINRES (tol 1e-4, MATLAB's default
+        maxit of 20) warm-started from the previous x, as discrep.m:50-66.
+        """
         data = np.asarray(data)
         nc, _, _ = self._raw_shape(data)
         data = data.reshape(self.M, nc, order="F")
@@ -359,8 +400,9 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
             raise ValueError("stddev must be a scalar finite nonnegative number")
         discrepancy = stddev * math.sqrt(data.size)
         damp = 0.1
+        x = None
         for _ in range(iters):
-            x = self.iNUFT(data, maxit if maxit is not None else 100, damp, None, solver=solver, tol=1e-4)
+            x = self.iNUFT(data, maxit, damp, None, solver=solver, tol=1e-4, x0=x)
             resnorm = float(np.linalg.norm(self.fNUFT(x) - data))
             damp = damp * (discrepancy / resnorm)
         return damp

@@ -336,8 +336,47 @@ class NufftRef:
             raise ValueError("W must be finite and nonnegative")
         return W
 
-    def iNUFT(self, raw, maxit=20, damp=0.0, W=None, solver="minres", tol=1e-4):
-        """iNUFT.m:25-138 default path; per-coil systems; returns (N1,N2,N3,nc)."""
+    def iNUFT_phase(self, raw, maxit, damp, lam, W=None, tol=1e-4):
+        """iNUFT.m:140-168 'phase-constraint' with pprojection (nufft_3d.m:325-334).
+
+        x from the plain MINRES solve; P = exp(i angle(convn(x, ones(3),
+        'same'))) -- ones(3) is 3x3, so the box runs over x-y per slice with
+        zero padding; then (P'A'WAP + damp^2 + i lam^2 imag) y = P'A'W raw by
+        CG with real inner products from y = 0 (the reference's pcgpc is
+        external); returns P y."""
+        x = self.iNUFT(raw, maxit, damp, W, solver="minres", tol=tol)
+        if maxit <= 1:
+            return x
+        N = self.N
+        nc = x.shape[3]
+        raw = np.asarray(raw, dtype=np.complex128).reshape(self.M, nc, order="F")
+        Wv = self.weights(W, None, None)
+        P = np.zeros_like(x)
+        pad = np.pad(x, ((1, 1), (1, 1), (0, 0), (0, 0)))
+        for dx in range(3):
+            for dy in range(3):
+                P += pad[dx:dx + N[0], dy:dy + N[1]]
+        P = np.exp(1j * np.angle(P))
+        b = np.conj(P) * self.aNUFT(Wv[:, None] * raw)
+        n = int(np.prod(N))
+        out = np.zeros((n, nc), dtype=np.complex128)
+        self.last_iters = []
+        for c in range(nc):
+            Pc = P[..., c].reshape(n, order="F")
+
+            def A(y, Pc=Pc):
+                t = self.iprojection(Pc * y, damp, Wv)[:, 0]
+                return np.conj(Pc) * t + 1j * lam ** 2 * y.imag
+            y, it = cg(A, b[..., c].reshape(n, order="F"), tol, maxit)
+            self.last_iters.append(it)
+            out[:, c] = Pc * y
+        return out.reshape(N[0], N[1], N[2], nc, order="F")
+
+    def iNUFT(self, raw, maxit=20, damp=0.0, W=None, solver="minres", tol=1e-4, x0=None):
+        """iNUFT.m:25-138 default path; per-coil systems; returns (N1,N2,N3,nc).
+
+        x0 (N1,N2,N3,nc) starts each solve from an earlier image, as the
+        minres(..., x) call of discrep.m:58 does."""
         raw = np.asarray(raw, dtype=np.complex128)
         nr = ny = None
         if raw.shape[0] == self.M:
@@ -357,13 +396,15 @@ class NufftRef:
             return self.aNUFT(Wv[:, None] * raw)
         b = self.aNUFT(Wv[:, None] * raw).reshape(int(np.prod(N)), nc, order="F")
         out = np.zeros_like(b)
+        X0 = None if x0 is None else np.asarray(x0, dtype=np.complex128).reshape(int(np.prod(N)), nc, order="F")
         self.last_iters = []
         for c in range(nc):
             A = lambda v: self.iprojection(v, damp, Wv)[:, 0]
+            xc = None if X0 is None else X0[:, c]
             if solver == "minres":
-                x, it = minres(A, b[:, c], tol, maxit)
+                x, it = minres(A, b[:, c], tol, maxit, xc)
             else:
-                x, it = cg(A, b[:, c], tol, maxit)
+                x, it = cg(A, b[:, c], tol, maxit, xc)
             self.last_iters.append(it)
             out[:, c] = x
         return out.reshape(N[0], N[1], N[2], nc, order="F")
@@ -390,10 +431,24 @@ class NufftRef:
         return out
 
 
-def cg(A, b, tol, maxit):
-    """Conjugate gradients with FP64 scalars, x0 = 0, relres stop (tol=0: fixed count)."""
-    x = np.zeros_like(b)
-    r = b.copy()
+def discrep(ref, data, stddev, iters=20, maxit=20, solver="minres"):
+    """discrep.m:2-69: damp <- damp * discrepancy/|A x - data|, 20 times, x
+    from MINRES (tol 1e-4, maxit 20) warm-started from the previous x."""
+    data = np.asarray(data, dtype=np.complex128).reshape(ref.M, -1, order="F")
+    discrepancy = stddev * math.sqrt(data.size)
+    damp, x = 0.1, None
+    for _ in range(iters):
+        x = ref.iNUFT(data, maxit, damp, None, solver=solver, tol=1e-4, x0=x)
+        resnorm = float(np.linalg.norm(ref.fNUFT(x) - data))
+        damp = damp * (discrepancy / resnorm)
+    return damp
+
+
+def cg(A, b, tol, maxit, x0=None):
+    """Conjugate gradients with FP64 scalars from x0 (default 0); stop when
+    |r| <= tol*|b| (tol=0: fixed count)."""
+    x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=b.dtype)
+    r = b.copy() if x0 is None else b - A(x)
     p = r.copy()
     rr = np.vdot(r, r).real
     nb = math.sqrt(np.vdot(b, b).real)
@@ -411,20 +466,24 @@ def cg(A, b, tol, maxit):
     return x, it
 
 
-def minres(A, b, tol, maxit):
-    """MINRES (Paige & Saunders 1975) for Hermitian A, x0 = 0, no preconditioner.
+def minres(A, b, tol, maxit, x0=None):
+    """MINRES (Paige & Saunders 1975) for Hermitian A from x0 (default 0), no
+    preconditioner; with x0 the recurrence runs on r0 = b - A x0 and x0 is
+    added to its iterate (MATLAB minres with x0).
 
     Lanczos order: p = A v - beta v_prev; alpha = <v, p>; p -= alpha v.
     Stops when the recurrence's residual estimate satisfies ||r||/||b|| <= tol
     (the relres test of iNUFT.m:114,136); tol=0 forces exactly ``maxit`` steps.
     Scalars are FP64.
     """
-    x = np.zeros_like(b)
-    beta1 = math.sqrt(np.vdot(b, b).real)
+    x = np.zeros_like(b) if x0 is None else np.array(x0, dtype=b.dtype)
+    r0 = b if x0 is None else b - A(x)
+    nb = math.sqrt(np.vdot(b, b).real)
+    beta1 = math.sqrt(np.vdot(r0, r0).real)
     if beta1 == 0:
         return x, 0
     v_prev = np.zeros_like(b)
-    v = b / beta1
+    v = r0 / beta1
     beta = beta1
     w1 = np.zeros_like(b)
     w2 = np.zeros_like(b)
@@ -456,7 +515,7 @@ def minres(A, b, tol, maxit):
         if beta_next > 0:
             v = p / beta_next
         beta = beta_next
-        if tol > 0 and phibar <= tol * beta1:
+        if tol > 0 and phibar <= tol * nb:
             break
         if beta_next == 0:
             break

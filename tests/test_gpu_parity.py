@@ -212,3 +212,68 @@ def test_fft_lengths_non_cubic(cuda, N, nc):
     y = rng.standard_normal((M, nc)) + 1j * rng.standard_normal((M, nc))
     assert rel(k_from_dev(obj.fNUFT(img_to_dev(torch, x))), ref.fNUFT(x)) < TOL_OP
     assert rel(img_from_dev(obj.aNUFT(k_to_dev(torch, y))), ref.aNUFT(y)) < TOL_OP
+
+
+@pytest.mark.parametrize("solver", ["minres", "cg"])
+def test_warm_start_matches_oracle(cuda, solver):
+    """nufft3d_inverse_x0 (host and device pointers) against the oracle started
+    from the same x0, fixed iteration count."""
+    torch = cuda
+    rng = np.random.default_rng(12)
+    N, M = 16, 3000
+    om = rng.uniform(-N / 2, N / 2 - 1, size=(3, M))
+    obj = nufft_3d(om, N, "J", 6)
+    ref = NufftRef(om, N, J=6)
+    raw = rng.standard_normal((M, 2)) + 1j * rng.standard_normal((M, 2))
+    x0 = ref.iNUFT(raw, 3, 0.1, solver=solver, tol=0)
+    imr = ref.iNUFT(raw, 5, 0.1, solver=solver, tol=0, x0=x0)
+    im = obj.iNUFT(raw, 5, 0.1, solver=solver, tol=0, x0=x0)
+    assert rel(im, imr) < TOL_IMG
+    imd = img_from_dev(obj.iNUFT(k_to_dev(torch, raw), 5, 0.1, solver=solver, tol=0, x0=img_to_dev(torch, x0)))
+    assert rel(imd, imr) < TOL_IMG
+    # warm start from the converged answer stops at once with tol > 0
+    xs = ref.iNUFT(raw, 200, 0.1, solver=solver, tol=1e-10)
+    _, its = obj.iNUFT(raw, 50, 0.1, solver=solver, tol=1e-3, x0=xs, return_iters=True)
+    assert max(its) <= 2
+
+
+def test_discrep_matches_oracle(cuda):
+    """discrep.m: 20 damp updates with warm-started MINRES solves."""
+    from oracle.nufft_ref import discrep as discrep_ref
+    rng = np.random.default_rng(13)
+    N, M = 16, 4000
+    om = rng.uniform(-N / 2, N / 2 - 1, size=(3, M))
+    obj = nufft_3d(om, N, "J", 6)
+    ref = NufftRef(om, N, J=6)
+    x = synth.phantom_with_phase(N)
+    data = ref.fNUFT(x)[:, 0]
+    sd = 0.05 * float(np.std(np.abs(data)))
+    data = data + sd * (rng.standard_normal(M) + 1j * rng.standard_normal(M)) / math.sqrt(2)
+    d_gpu = obj.discrep(data, sd)
+    d_ref = discrep_ref(ref, data, sd)
+    assert abs(d_gpu - d_ref) / d_ref < 1e-2, (d_gpu, d_ref)
+
+
+def test_phase_constraint_matches_oracle(cuda):
+    """iNUFT 'phase-constraint' (iNUFT.m:140-168, pprojection nufft_3d.m:325-334)
+    on a phantom with smooth phase, host and device paths, fixed iteration
+    counts.  Tolerance 1e-3: the phase map is taken from the FP32 MINRES image,
+    and voxels where the 3x3 box sum is near zero carry FP32-sized phase
+    differences into the second solve."""
+    torch = cuda
+    N = 16
+    om = synth.koosh_ball(N, 16, 600)
+    obj = nufft_3d(om, N, "J", 6)
+    ref = NufftRef(om, N, J=6)
+    x = synth.phantom_with_phase(N)
+    raw = np.concatenate([ref.fNUFT(x), ref.fNUFT(x * np.exp(0.3j))], axis=1)
+    imr = ref.iNUFT_phase(raw, 6, 0.05, 0.5, tol=0)
+    im = obj.iNUFT(raw, 6, 0.05, constraint="phase-constraint", lam=0.5, tol=0)
+    assert rel(im, imr) < 1e-3
+    imd = img_from_dev(obj.iNUFT(k_to_dev(torch, raw), 6, 0.05, constraint="phase-constraint", lam=0.5, tol=0))
+    assert rel(imd, im) < 1e-5
+    with pytest.raises(ValueError):
+        obj.iNUFT(raw, 6, 0.05, constraint="phase-constraint")      # lambda required
+    with pytest.warns(UserWarning):
+        plain = obj.iNUFT(raw, 1, 0.05, constraint="phase-constraint", lam=0.5, tol=0)
+    assert rel(plain, obj.iNUFT(raw, 1, 0.05, tol=0)) < 1e-6

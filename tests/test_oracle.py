@@ -187,3 +187,22 @@ def test_golden_fixtures_reproduce(path):
     assert np.linalg.norm(a - z["a"]) / np.linalg.norm(z["a"]) < 1e-6
     np.testing.assert_allclose(ref.U, z["U"], rtol=1e-6)
     np.testing.assert_allclose(ref.d, z["d"], rtol=1e-5, atol=1e-6)
+
+
+def test_warm_start_solvers():
+    """minres/cg from x0: the exact solution stops at once; any x0 reaches the
+    same solution; the stop test stays relative to |b| (MATLAB semantics)."""
+    from oracle.nufft_ref import cg, minres
+    rng = np.random.default_rng(11)
+    n = 40
+    Q = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    H = Q @ Q.conj().T + n * np.eye(n)
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    A = lambda v: H @ v
+    xs = np.linalg.solve(H, b)
+    for solver in (minres, cg):
+        x, it = solver(A, b, 1e-10, 200, xs)
+        assert it <= 1 and np.allclose(x, xs)
+        x0 = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        x, _ = solver(A, b, 1e-12, 200, x0)
+        assert np.linalg.norm(x - xs) / np.linalg.norm(xs) < 1e-9
