@@ -193,8 +193,8 @@ int nufft3d_inverse_x0_host(nufft3d_plan *plan, const float *raw_host, float *x_
  * No single counterpart in the reference, which handles one object at a time;
  * each volume's result equals what fNUFT / aNUFT / iNUFT of its own plan
  * gives.  plans[v] must be distinct handles (nufft3d_plan_share for repeated
- * trajectories) sharing ceil(J/2), the kernel type and 2-D/3-D; the batch uses
- * their work buffers, so do not use those handles concurrently with it. */
+ * trajectories) sharing the kernel (J, u, alpha, radial) and 2-D/3-D; the batch
+ * uses their work buffers, so do not use those handles concurrently with it. */
 typedef struct nufft3d_batch nufft3d_batch;
 int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, int nvol, nufft3d_batch **batch);
 int nufft3d_batch_destroy(nufft3d_batch *batch);

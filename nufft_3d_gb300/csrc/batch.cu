@@ -53,9 +53,12 @@ struct nufft3d_batch {
         int4 *tab;
         int n;
         size_t smem;
+        int r1 = 0;  // > 0: strided pass by the register four-step FFT (K = 16 r1)
     };
     std::vector<FGroup> fgroups[NFFT];
     BatchInterp *gat = nullptr, *spr = nullptr;
+    std::vector<CUtensorMap> h_tmaps;   // [nvol][4] gather maps (coil widths 1, 2, 4, 8)
+    CUtensorMap *d_tmaps = nullptr;     // their device copy (start of the descriptor buffer)
     std::vector<BatchInterp> h_gat, h_spr;
     // interpolation launch groups: one per coil-pass width
     struct IGroup {
@@ -271,10 +274,12 @@ static int64_t fft_blocks(const nufft3d_plan *p, const BatchFFT &d, int stage, i
 
 static int upload(nufft3d_batch *b, cudaStream_t s)
 {
-    // host staging layout: fft[0..5], gat, spr, pout, pin
+    // host staging layout: gather tensor maps, fft[0..5], gat, spr, pout, pin
     size_t off = 0;
     char *h = static_cast<char *>(b->stage);
     NUFFT_CUDA_TRY(cudaEventSynchronize(b->up_done));  // previous upload has left the staging buffer
+    std::memcpy(h, b->h_tmaps.data(), b->h_tmaps.size() * sizeof(CUtensorMap));
+    off += b->h_tmaps.size() * sizeof(CUtensorMap);
     for (int st = 0; st < NFFT; ++st) {
         const size_t n = b->h_fft[st].size() * sizeof(BatchFFT);
         std::memcpy(h + off, b->h_fft[st].data(), n);
@@ -328,6 +333,12 @@ static void set_io(nufft3d_batch *b, int mode, const float2 *const *in, float2 *
         BatchInterp &g = b->h_gat[v];
         g.in = S.G;
         g.out = S.ks;
+        // bulk tile copies: maps of this call's grid (encoded per call, so a
+        // grid reallocated between calls never leaves a stale map)
+        g.tmap_ok = 0;
+        g.tmaps = b->d_tmaps + 4 * v;
+        for (int lw = 1; lw < 4; ++lw)
+            if (encode_gather_map(p, S.G, b->nc[v], 1 << lw, &b->h_tmaps[4 * v + lw])) g.tmap_ok |= 1 << lw;
         g.scale = mode == 2 ? (float)(1.0 / (double)p->nnz) : (float)(1.0 / std::sqrt((double)p->nnz));
         g.wsample = mode == 2 ? p->d : nullptr;
         BatchInterp &sp = b->h_spr[v];
@@ -356,14 +367,20 @@ static int zero_grids(nufft3d_batch *b, cudaStream_t s)
 
 static int run_fft_stage(nufft3d_batch *b, int st, int kind, cudaStream_t s)
 {
-    for (auto &g : b->fgroups[st]) NUFFT_TRY(launch_fft_batch(b->fft[st], g.tab, g.n, kind, g.smem, b->rare, s));
+    for (auto &g : b->fgroups[st]) {
+        if (kind == 1 && g.r1)
+            NUFFT_TRY(launch_fft_batch4(b->fft[st], g.tab, g.n, g.r1, s));
+        else
+            NUFFT_TRY(launch_fft_batch(b->fft[st], g.tab, g.n, kind, g.smem, b->rare, s));
+    }
     return NUFFT3D_SUCCESS;
 }
 
 static int run_interp(nufft3d_batch *b, bool gather, cudaStream_t s)
 {
     for (auto &g : b->igroups)
-        NUFFT_TRY(launch_interp_batch(gather, g.cb, b->R, b->radial, gather ? b->gat : b->spr, g.tab, g.n, g.smem, s));
+        NUFFT_TRY(launch_interp_batch(gather, g.cb, b->R, b->radial, gather ? b->gat : b->spr, g.tab, g.n, g.smem,
+                                      b->plans[0]->kb, s));
     return NUFFT3D_SUCCESS;
 }
 
@@ -408,8 +425,10 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
                 return fail(NUFFT3D_ERR_ARG, "a batch needs one plan handle per volume (use nufft3d_plan_share)");
         if (plans[v]->device != plans[0]->device) return fail(NUFFT3D_ERR_ARG, "batch plans on different devices");
         if (plans[v]->geom.R != plans[0]->geom.R || plans[v]->geom.radial != plans[0]->geom.radial ||
-            plans[v]->geom.is2d != plans[0]->geom.is2d)
-            return fail(NUFFT3D_ERR_UNSUPPORTED, "batch volumes must share ceil(J/2), the kernel type and 2-D/3-D");
+            plans[v]->geom.is2d != plans[0]->geom.is2d ||
+            std::memcmp(&plans[v]->kb, &plans[0]->kb, sizeof(KBParams)) != 0)
+            return fail(NUFFT3D_ERR_UNSUPPORTED,
+                        "batch volumes must share the kernel (J, u, alpha, radial) and 2-D/3-D");
     }
     NUFFT_DEVICE_LOCK;
     int prev = -1;
@@ -455,6 +474,7 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
         b->h_fft[st].resize(nvol);
         std::vector<std::pair<int, std::vector<int4>>> groups;  // (K, table)
         std::vector<size_t> gsmem;
+        std::vector<char> gvec16;  // every volume of the group has 16-wide line chunks
         for (int v = 0; v < nvol; ++v) {
             fill_fft(b, v, &b->h_fft[st][v], st);
             const BatchFFT &d = b->h_fft[st][v];
@@ -463,7 +483,9 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             if (gi == groups.size()) {
                 groups.push_back({d.fd.n, {}});
                 gsmem.push_back(0);
+                gvec16.push_back(1);
             }
+            if (st != FX && st != IX && d.lp.vec != 16) gvec16[gi] = 0;
             std::vector<int4> &tab = groups[gi].second;
             if (st == FX || st == IX) {
                 const int nch = (nc[v] + kMaxLineCoilsHost - 1) / kMaxLineCoilsHost;
@@ -480,6 +502,7 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             nufft3d_batch::FGroup fg;
             fg.n = (int)groups[gi].second.size();
             fg.smem = gsmem[gi];
+            fg.r1 = (st == FX || st == IX) ? 0 : batch_four_step(groups[gi].first, gvec16[gi] != 0);
             int s2 = dalloc(b, &fg.tab, groups[gi].second.size());
             if (s2 != NUFFT3D_SUCCESS) return bail(s2);
             if (fg.n && cudaMemcpy(fg.tab, groups[gi].second.data(), fg.n * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess)
@@ -562,14 +585,17 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             return bail(fail(NUFFT3D_ERR_CUDA, "batch table upload failed"));
     }
     // one device buffer for all descriptors, mirrored by pinned staging
-    size_t bytes = NFFT * nvol * sizeof(BatchFFT) + 2 * nvol * sizeof(BatchInterp) + 2 * nvol * sizeof(BatchPerm);
+    b->h_tmaps.assign((size_t)4 * nvol, CUtensorMap{});
+    size_t bytes = 4 * nvol * sizeof(CUtensorMap) + NFFT * nvol * sizeof(BatchFFT) + 2 * nvol * sizeof(BatchInterp) +
+                   2 * nvol * sizeof(BatchPerm);
     b->stage_bytes = bytes;
     if (cudaMallocHost(&b->stage, bytes) != cudaSuccess) return bail(fail(NUFFT3D_ERR_NOMEM, "batch staging"));
     char *base = nullptr;
     int s2 = dalloc(b, &base, bytes);
     if (s2 != NUFFT3D_SUCCESS) return bail(s2);
     b->dstage = base;
-    size_t off = 0;
+    b->d_tmaps = reinterpret_cast<CUtensorMap *>(base);  // cudaMalloc alignment covers the 64-byte rule
+    size_t off = 4 * nvol * sizeof(CUtensorMap);
     for (int st = 0; st < NFFT; ++st) {
         b->fft[st] = reinterpret_cast<BatchFFT *>(base + off);
         off += nvol * sizeof(BatchFFT);

@@ -262,17 +262,16 @@ template <> __device__ __forceinline__ void dft_reg<24>(float2 (&u)[24]) { dft_c
 // keeps global accesses coalesced (a line is one complex of a contiguous row)
 // and the row stride K+1 keeps shared-memory accesses conflict-free.
 template <int R1>
-__global__ void __launch_bounds__(384)
-k_line4(const float2 *__restrict__ in, float2 *__restrict__ out, LinePass lp, const float2 *__restrict__ twg,
-        int inv)
+__device__ __forceinline__ void line4_body(const float2 *__restrict__ in, float2 *__restrict__ out,
+                                           const LinePass &lp, const float2 *__restrict__ twg, int inv, int blk,
+                                           float2 *sm)
 {
     constexpr int R2 = 16, K = R1 * R2, L = 16, LS = K + 1;
-    extern __shared__ float2 sm[];
     float2 *Y = sm;
     float2 *tw = sm + L * LS;
     for (int t = threadIdx.x; t < K; t += blockDim.x) tw[t] = twg[t];
-    const int outer = blockIdx.x / lp.nchunks;
-    const int chunk = blockIdx.x - outer * lp.nchunks;
+    const int outer = blk / lp.nchunks;
+    const int chunk = blk - outer * lp.nchunks;
     const float2 *ib = in + outer * lp.in_outer_stride + (int64_t)chunk * L;
     float2 *ob = out + outer * lp.out_outer_stride + (int64_t)chunk * L;
     const float sg = inv ? -1.f : 1.f;
@@ -321,6 +320,27 @@ k_line4(const float2 *__restrict__ in, float2 *__restrict__ out, LinePass lp, co
             }
         }
     }
+}
+
+template <int R1>
+__global__ void __launch_bounds__(384)
+k_line4(const float2 *__restrict__ in, float2 *__restrict__ out, LinePass lp, const float2 *__restrict__ twg,
+        int inv)
+{
+    extern __shared__ float2 sm[];
+    line4_body<R1>(in, out, lp, twg, inv, blockIdx.x, sm);
+}
+
+// Batched strided passes of one transform length: block -> (volume, block)
+template <int R1>
+__global__ void __launch_bounds__(384)
+k_line4_batch(const BatchFFT *__restrict__ vols, const int4 *__restrict__ table)
+{
+    extern __shared__ float2 sm[];
+    const int4 e = table[blockIdx.x];
+    const BatchFFT &b = vols[e.x];
+    const LinePass lp = b.lp;  // in registers: the loops read the strides per element
+    line4_body<R1>(b.in, b.out, lp, b.fd.tw, b.inv, e.y, sm);
 }
 
 static int four_step_r1(int K, int vec)
@@ -581,14 +601,41 @@ __global__ void __launch_bounds__(kFftThreads)
 k_fft_batch(const BatchFFT *__restrict__ vols, const int4 *__restrict__ table, int kind)
 {
     extern __shared__ float2 sm[];
+    // the volume's descriptor is copied to shared memory once per block: the
+    // FFT passes read its radix list and strides many times, which from
+    // global memory (unlike a kernel parameter) costs a load each time
+    __shared__ BatchFFT d;
     const int4 e = table[blockIdx.x];
-    const BatchFFT &b = vols[e.x];
+    if (threadIdx.x == 0) d = vols[e.x];
+    __syncthreads();
     if (kind == 0)
-        fx_body<RARE>(b.in, b.U, b.out, b.N1, b.N23, b.nc, b.fd, e.y, e.z, sm);
+        fx_body<RARE>(d.in, d.U, d.out, d.N1, d.N23, d.nc, d.fd, e.y, e.z, sm);
     else if (kind == 1)
-        line_body<RARE>(b.in, b.out, b.lp, b.fd, b.inv, e.y, sm);
+        line_body<RARE>(d.in, d.out, d.lp, d.fd, d.inv, e.y, sm);
     else
-        ix_body<RARE>(b.in, b.U, b.out, b.N1, b.N23, b.nc, b.fd, b.scale, b.addend, b.add_coef, e.y, e.z, sm);
+        ix_body<RARE>(d.in, d.U, d.out, d.N1, d.N23, d.nc, d.fd, d.scale, d.addend, d.add_coef, e.y, e.z, sm);
+}
+
+// Four-step radix R1 (K = 16 R1) of a strided-pass group whose volumes all
+// have 16-wide line chunks, else 0.
+int batch_four_step(int K, bool all_vec16) { return all_vec16 ? four_step_r1(K, 16) : 0; }
+
+size_t batch_four_step_smem(int K) { return line4_smem(K); }
+
+int launch_fft_batch4(const BatchFFT *vols, const int4 *table, int nblocks, int r1, cudaStream_t s)
+{
+    if (nblocks <= 0) return NUFFT3D_SUCCESS;
+    const int threads = 16 * (r1 > 16 ? r1 : 16);
+    const size_t smem = line4_smem(16 * r1);
+    switch (r1) {
+    case 8: k_line4_batch<8><<<nblocks, threads, smem, s>>>(vols, table); break;
+    case 12: k_line4_batch<12><<<nblocks, threads, smem, s>>>(vols, table); break;
+    case 16: k_line4_batch<16><<<nblocks, threads, smem, s>>>(vols, table); break;
+    case 20: k_line4_batch<20><<<nblocks, threads, smem, s>>>(vols, table); break;
+    default: k_line4_batch<24><<<nblocks, threads, smem, s>>>(vols, table); break;
+    }
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
 }
 
 int launch_fft_batch(const BatchFFT *vols, const int4 *table, int nblocks, int kind, size_t smem, bool rare,
@@ -670,22 +717,38 @@ int launch_iy(nufft3d_plan *p, const float2 *B2, float2 *B1, int nc, cudaStream_
                        K2 * row, N2 * row, p->fft[1], 1, s);
 }
 
+// Allow each FFT kernel all the shared memory a block can have, less its
+// static part.
+template <typename Kern>
+static int allow_fft_smem(Kern kernel)
+{
+    cudaFuncAttributes fa;
+    NUFFT_CUDA_TRY(cudaFuncGetAttributes(&fa, kernel));
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        227 * 1024 - (int)fa.sharedSizeBytes));
+    return NUFFT3D_SUCCESS;
+}
+
 int configure_fft_kernels()
 {
-    const int max_smem = 227 * 1024;
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fx<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_ix<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fx<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_ix<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fft_batch<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_fft_batch<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line4<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line4<12>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line4<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line4<20>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_line4<24>, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    NUFFT_TRY(allow_fft_smem(k_fx<false>));
+    NUFFT_TRY(allow_fft_smem(k_ix<false>));
+    NUFFT_TRY(allow_fft_smem(k_line<false>));
+    NUFFT_TRY(allow_fft_smem(k_fx<true>));
+    NUFFT_TRY(allow_fft_smem(k_ix<true>));
+    NUFFT_TRY(allow_fft_smem(k_line<true>));
+    NUFFT_TRY(allow_fft_smem(k_fft_batch<false>));
+    NUFFT_TRY(allow_fft_smem(k_fft_batch<true>));
+    NUFFT_TRY(allow_fft_smem(k_line4<8>));
+    NUFFT_TRY(allow_fft_smem(k_line4<12>));
+    NUFFT_TRY(allow_fft_smem(k_line4<16>));
+    NUFFT_TRY(allow_fft_smem(k_line4<20>));
+    NUFFT_TRY(allow_fft_smem(k_line4<24>));
+    NUFFT_TRY(allow_fft_smem(k_line4_batch<8>));
+    NUFFT_TRY(allow_fft_smem(k_line4_batch<12>));
+    NUFFT_TRY(allow_fft_smem(k_line4_batch<16>));
+    NUFFT_TRY(allow_fft_smem(k_line4_batch<20>));
+    NUFFT_TRY(allow_fft_smem(k_line4_batch<24>));
     return configure_fft_constants();
 }
 

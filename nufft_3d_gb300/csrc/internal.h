@@ -1,6 +1,7 @@
 // Internal declarations shared by the libnufft3d translation units.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <memory>
@@ -170,6 +171,8 @@ struct BatchInterp {
     Geom g;
     KBParams kb;
     Cand cand;
+    const CUtensorMap *tmaps;  // gather: [4] maps of the grid for coil widths 1, 2, 4, 8 (device memory)
+    int tmap_ok;               // bit log2(width): that map is valid
     int nc;
     float scale;
 };
@@ -190,10 +193,13 @@ int line_vec(int64_t rowlen);
 size_t line_smem(int vec, int K);
 bool needs_rare(const FFTDesc &f);
 constexpr int kMaxLineCoilsHost = 16;
+int batch_four_step(int K, bool all_vec16);
+size_t batch_four_step_smem(int K);
+int launch_fft_batch4(const BatchFFT *vols, const int4 *table, int nblocks, int r1, cudaStream_t s);
 int launch_fft_batch(const BatchFFT *vols, const int4 *table, int nblocks, int kind, size_t smem, bool rare,
                      cudaStream_t s);
 int launch_interp_batch(bool gather, int cb, int R, bool radial, const BatchInterp *vols, const int4 *table,
-                        int nblocks, size_t smem, cudaStream_t s);
+                        int nblocks, size_t smem, const KBParams &kb, cudaStream_t s);
 int launch_perm_batch(bool out, const BatchPerm *vols, const int4 *table, int nblocks, cudaStream_t s);
 
 // ----------------------------------------------------------------- plan
@@ -337,7 +343,8 @@ int run_inverse(nufft3d_plan *p, const float2 *raw, float2 *x, int nc, int maxit
 
 size_t smem_interp_bytes(const Geom &g, int cb);
 size_t cand_smem_bytes(int n);
-int interp_check_error();  // reads and clears the interpolation timeout flag
+int interp_check_error();
+bool encode_gather_map(const nufft3d_plan *p, const float2 *G, int nc, int cb, CUtensorMap *m);  // reads and clears the interpolation timeout flag
 size_t smem_plane_bytes(int R, int cb);
 
 // Stage timing scope: records an event pair on stream s when profiling is on

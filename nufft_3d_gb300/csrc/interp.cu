@@ -686,19 +686,24 @@ __global__ void k_permute_in(const float2 *__restrict__ k, float2 *__restrict__ 
 // `table`; one launch covers every volume of a batch.
 template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
-k_gather_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ table)
+k_gather_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ table, KBParams kb)
 {
     extern __shared__ float4 smem4[];
     const int4 e = table[blockIdx.x];
     const BatchInterp &b = vols[e.x];
     const Cand &cd = b.cand;
-    gather_body<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, b.kb, b.scale, b.wsample,
-                               cd, smem4, nullptr, nullptr);
+    __shared__ unsigned long long bar;
+    constexpr int lw = CB >= 8 ? 3 : CB >= 4 ? 2 : CB >= 2 ? 1 : 0;
+    const CUtensorMap *tm = (b.tmap_ok >> lw) & 1 ? &b.tmaps[lw] : nullptr;
+    // the kernel weights are evaluated per tap, so they come from the
+    // parameter bank (every volume of a batch shares them), not the descriptor
+    gather_body<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, kb, b.scale, b.wsample, cd,
+                               smem4, tm, &bar);
 }
 
 template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
-k_spread_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ table)
+k_spread_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ table, KBParams kb)
 {
     extern __shared__ float4 smem4[];
     __shared__ float red[33];
@@ -706,8 +711,7 @@ k_spread_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ ta
     const int4 e = table[blockIdx.x];
     const BatchInterp &b = vols[e.x];
     const Cand &cd = b.cand;
-    spread_body<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, b.kb, cd, smem4, red,
-                               queues);
+    spread_body<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, kb, cd, smem4, red, queues);
 }
 
 // Batched permutes: block -> (volume, chunk of 256 samples).
@@ -795,6 +799,18 @@ static bool gather_tensor_map(const nufft3d_plan *p, const float2 *G, int nc, CU
     return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<float2 *>(G), dim, str, box, es,
                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Encodes the gather tensor map of grid G (nc coils) for chunks of cb
+// coils; false where the bulk copy does not apply.
+bool encode_gather_map(const nufft3d_plan *p, const float2 *G, int nc, int cb, CUtensorMap *m)
+{
+    switch (cb) {
+    case 2: return gather_tensor_map<2>(p, G, nc, m);
+    case 4: return gather_tensor_map<4>(p, G, nc, m);
+    case 8: return gather_tensor_map<8>(p, G, nc, m);
+    default: return false;
+    }
 }
 
 int interp_check_error()
@@ -931,40 +947,40 @@ int launch_permute_in(nufft3d_plan *p, const float2 *k, float2 *ks, int nc,
 
 template <int CB, bool RADIAL, int R>
 static int interp_batch_t(bool gather, const BatchInterp *vols, const int4 *table, int nblocks, size_t smem,
-                          cudaStream_t s)
+                          const KBParams &kb, cudaStream_t s)
 {
     if (gather)
-        k_gather_batch<CB, RADIAL, R><<<nblocks, kInterpThreads, smem, s>>>(vols, table);
+        k_gather_batch<CB, RADIAL, R><<<nblocks, kInterpThreads, smem, s>>>(vols, table, kb);
     else
-        k_spread_batch<CB, RADIAL, R><<<nblocks, kInterpThreads, smem, s>>>(vols, table);
+        k_spread_batch<CB, RADIAL, R><<<nblocks, kInterpThreads, smem, s>>>(vols, table, kb);
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }
 
 template <int CB, bool RADIAL>
 static int interp_batch_r(bool gather, int R, const BatchInterp *vols, const int4 *table, int nblocks, size_t smem,
-                          cudaStream_t s)
+                          const KBParams &kb, cudaStream_t s)
 {
     switch (R) {
-    case 1: return interp_batch_t<CB, RADIAL, 1>(gather, vols, table, nblocks, smem, s);
-    case 2: return interp_batch_t<CB, RADIAL, 2>(gather, vols, table, nblocks, smem, s);
-    case 3: return interp_batch_t<CB, RADIAL, 3>(gather, vols, table, nblocks, smem, s);
-    default: return interp_batch_t<(CB < 8 ? CB : 4), RADIAL, 4>(gather, vols, table, nblocks, smem, s);
+    case 1: return interp_batch_t<CB, RADIAL, 1>(gather, vols, table, nblocks, smem, kb, s);
+    case 2: return interp_batch_t<CB, RADIAL, 2>(gather, vols, table, nblocks, smem, kb, s);
+    case 3: return interp_batch_t<CB, RADIAL, 3>(gather, vols, table, nblocks, smem, kb, s);
+    default: return interp_batch_t<(CB < 8 ? CB : 4), RADIAL, 4>(gather, vols, table, nblocks, smem, kb, s);
     }
 }
 
 int launch_interp_batch(bool gather, int cb, int R, bool radial, const BatchInterp *vols, const int4 *table,
-                        int nblocks, size_t smem, cudaStream_t s)
+                        int nblocks, size_t smem, const KBParams &kb, cudaStream_t s)
 {
     if (nblocks <= 0) return NUFFT3D_SUCCESS;
-    if (cb >= 8) return radial ? interp_batch_r<8, true>(gather, R, vols, table, nblocks, smem, s)
-                               : interp_batch_r<8, false>(gather, R, vols, table, nblocks, smem, s);
-    if (cb >= 4) return radial ? interp_batch_r<4, true>(gather, R, vols, table, nblocks, smem, s)
-                               : interp_batch_r<4, false>(gather, R, vols, table, nblocks, smem, s);
-    if (cb >= 2) return radial ? interp_batch_r<2, true>(gather, R, vols, table, nblocks, smem, s)
-                               : interp_batch_r<2, false>(gather, R, vols, table, nblocks, smem, s);
-    return radial ? interp_batch_r<1, true>(gather, R, vols, table, nblocks, smem, s)
-                  : interp_batch_r<1, false>(gather, R, vols, table, nblocks, smem, s);
+    if (cb >= 8) return radial ? interp_batch_r<8, true>(gather, R, vols, table, nblocks, smem, kb, s)
+                               : interp_batch_r<8, false>(gather, R, vols, table, nblocks, smem, kb, s);
+    if (cb >= 4) return radial ? interp_batch_r<4, true>(gather, R, vols, table, nblocks, smem, kb, s)
+                               : interp_batch_r<4, false>(gather, R, vols, table, nblocks, smem, kb, s);
+    if (cb >= 2) return radial ? interp_batch_r<2, true>(gather, R, vols, table, nblocks, smem, kb, s)
+                               : interp_batch_r<2, false>(gather, R, vols, table, nblocks, smem, kb, s);
+    return radial ? interp_batch_r<1, true>(gather, R, vols, table, nblocks, smem, kb, s)
+                  : interp_batch_r<1, false>(gather, R, vols, table, nblocks, smem, kb, s);
 }
 
 int launch_perm_batch(bool out, const BatchPerm *vols, const int4 *table, int nblocks, cudaStream_t s)

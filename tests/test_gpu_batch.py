@@ -63,5 +63,8 @@ def test_batch_rejects_mixed_kernels(cuda):
     b = nufft_3d(om, 16, "J", 4)
     with pytest.raises(Exception, match="share"):
         NufftBatch([a, a], [1, 1])
-    with pytest.raises(Exception, match="ceil"):
+    with pytest.raises(Exception, match="kernel"):
         NufftBatch([a, b], [1, 1])
+    c = nufft_3d(om, 16, "J", 6, "u", 1.5)   # same ceil(J/2), different alpha
+    with pytest.raises(Exception, match="kernel"):
+        NufftBatch([a.share(), c], [1, 1])
