@@ -54,6 +54,9 @@ struct nufft3d_batch {
         int n;
         size_t smem;
         int r1 = 0;  // > 0: strided pass by the register four-step FFT (K = 16 r1)
+        std::vector<int> vols;    // volumes of the group, in table order
+        std::vector<int> blocks;  // their block counts
+        std::vector<int> nch;     // their coil chunks per line (x passes)
     };
     std::vector<FGroup> fgroups[NFFT];
     BatchInterp *gat = nullptr, *spr = nullptr;
@@ -367,11 +370,25 @@ static int zero_grids(nufft3d_batch *b, cudaStream_t s)
 
 static int run_fft_stage(nufft3d_batch *b, int st, int kind, cudaStream_t s)
 {
+    // descriptors go by value as kernel parameters, kBatchParamVols volumes
+    // per launch (current host copies: set_io has filled this call's pointers)
+    BatchFFTParams P;
     for (auto &g : b->fgroups[st]) {
-        if (kind == 1 && g.r1)
-            NUFFT_TRY(launch_fft_batch4(b->fft[st], g.tab, g.n, g.r1, s));
-        else
-            NUFFT_TRY(launch_fft_batch(b->fft[st], g.tab, g.n, kind, g.smem, b->rare, s));
+        for (size_t i0 = 0; i0 < g.vols.size(); i0 += kBatchParamVols) {
+            std::memset(&P, 0, sizeof(P));
+            const size_t i1 = std::min(g.vols.size(), i0 + kBatchParamVols);
+            P.nvol = (int)(i1 - i0);
+            int acc = 0;
+            for (size_t i = i0; i < i1; ++i) {
+                const int j = (int)(i - i0);
+                P.first[j] = acc;
+                P.nch[j] = g.nch[i];
+                P.v[j] = b->h_fft[st][g.vols[i]];
+                acc += g.blocks[i];
+            }
+            P.first[P.nvol] = acc;
+            NUFFT_TRY(launch_fft_batch_p(P, kind, g.smem, b->rare, kind == 1 ? g.r1 : 0, s));
+        }
     }
     return NUFFT3D_SUCCESS;
 }
@@ -475,6 +492,7 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
         std::vector<std::pair<int, std::vector<int4>>> groups;  // (K, table)
         std::vector<size_t> gsmem;
         std::vector<char> gvec16;  // every volume of the group has 16-wide line chunks
+        std::vector<std::vector<int>> gvols, gblocks, gnch;
         for (int v = 0; v < nvol; ++v) {
             fill_fft(b, v, &b->h_fft[st][v], st);
             const BatchFFT &d = b->h_fft[st][v];
@@ -487,13 +505,23 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             }
             if (st != FX && st != IX && d.lp.vec != 16) gvec16[gi] = 0;
             std::vector<int4> &tab = groups[gi].second;
+            gvols.resize(groups.size());
+            gvols[gi].push_back(v);
             if (st == FX || st == IX) {
                 const int nch = (nc[v] + kMaxLineCoilsHost - 1) / kMaxLineCoilsHost;
+                gblocks.resize(groups.size());
+                gnch.resize(groups.size());
+                gblocks[gi].push_back(d.N23 * nch);
+                gnch[gi].push_back(nch);
                 for (int line = 0; line < d.N23; ++line)
                     for (int c = 0; c < nch; ++c) tab.push_back(make_int4(v, line, c, 0));
                 gsmem[gi] = std::max(gsmem[gi], line_smem(std::min(nc[v], kMaxLineCoilsHost), d.fd.n));
             } else {
                 const int64_t nb = fft_blocks(plans[v], d, st, nc[v]);
+                gblocks.resize(groups.size());
+                gnch.resize(groups.size());
+                gblocks[gi].push_back((int)nb);
+                gnch[gi].push_back(1);
                 for (int64_t k = 0; k < nb; ++k) tab.push_back(make_int4(v, (int)k, 0, 0));
                 gsmem[gi] = std::max(gsmem[gi], line_smem(d.lp.vec, d.fd.n));
             }
@@ -503,6 +531,9 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             fg.n = (int)groups[gi].second.size();
             fg.smem = gsmem[gi];
             fg.r1 = (st == FX || st == IX) ? 0 : batch_four_step(groups[gi].first, gvec16[gi] != 0);
+            fg.vols = gvols[gi];
+            fg.blocks = gblocks[gi];
+            fg.nch = gnch[gi];
             int s2 = dalloc(b, &fg.tab, groups[gi].second.size());
             if (s2 != NUFFT3D_SUCCESS) return bail(s2);
             if (fg.n && cudaMemcpy(fg.tab, groups[gi].second.data(), fg.n * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess)

@@ -616,6 +616,69 @@ k_fft_batch(const BatchFFT *__restrict__ vols, const int4 *__restrict__ table, i
         ix_body<RARE>(d.in, d.U, d.out, d.N1, d.N23, d.nc, d.fd, d.scale, d.addend, d.add_coef, e.y, e.z, sm);
 }
 
+__device__ __forceinline__ int batch_volume(const BatchFFTParams &P, int blk)
+{
+    int lo = 0, hi = P.nvol - 1;  // largest v with first[v] <= blk
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P.first[mid] <= blk) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <bool RARE>
+__global__ void __launch_bounds__(kFftThreads)
+k_fft_batch_p(const __grid_constant__ BatchFFTParams P, int kind)
+{
+    extern __shared__ float2 sm[];
+    const int v = batch_volume(P, blockIdx.x);
+    const int k = blockIdx.x - P.first[v];
+    const BatchFFT &b = P.v[v];
+    if (kind == 1) {
+        line_body<RARE>(b.in, b.out, b.lp, b.fd, b.inv, k, sm);
+    } else {
+        const int line = k / P.nch[v], c = k - line * P.nch[v];
+        if (kind == 0)
+            fx_body<RARE>(b.in, b.U, b.out, b.N1, b.N23, b.nc, b.fd, line, c, sm);
+        else
+            ix_body<RARE>(b.in, b.U, b.out, b.N1, b.N23, b.nc, b.fd, b.scale, b.addend, b.add_coef, line, c, sm);
+    }
+}
+
+template <int R1>
+__global__ void __launch_bounds__(384)
+k_line4_batch_p(const __grid_constant__ BatchFFTParams P)
+{
+    extern __shared__ float2 sm[];
+    const int v = batch_volume(P, blockIdx.x);
+    const BatchFFT &b = P.v[v];
+    line4_body<R1>(b.in, b.out, b.lp, b.fd.tw, b.inv, blockIdx.x - P.first[v], sm);
+}
+
+int launch_fft_batch_p(const BatchFFTParams &P, int kind, size_t smem, bool rare, int r1, cudaStream_t s)
+{
+    const int nblocks = P.first[P.nvol];
+    if (nblocks <= 0) return NUFFT3D_SUCCESS;
+    if (kind == 1 && r1) {
+        const int threads = 16 * (r1 > 16 ? r1 : 16);
+        const size_t sm4 = line4_smem(16 * r1);
+        switch (r1) {
+        case 8: k_line4_batch_p<8><<<nblocks, threads, sm4, s>>>(P); break;
+        case 12: k_line4_batch_p<12><<<nblocks, threads, sm4, s>>>(P); break;
+        case 16: k_line4_batch_p<16><<<nblocks, threads, sm4, s>>>(P); break;
+        case 20: k_line4_batch_p<20><<<nblocks, threads, sm4, s>>>(P); break;
+        default: k_line4_batch_p<24><<<nblocks, threads, sm4, s>>>(P); break;
+        }
+    } else if (rare) {
+        k_fft_batch_p<true><<<nblocks, kFftThreads, smem, s>>>(P, kind);
+    } else {
+        k_fft_batch_p<false><<<nblocks, kFftThreads, smem, s>>>(P, kind);
+    }
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
 // Four-step radix R1 (K = 16 R1) of a strided-pass group whose volumes all
 // have 16-wide line chunks, else 0.
 int batch_four_step(int K, bool all_vec16) { return all_vec16 ? four_step_r1(K, 16) : 0; }
@@ -749,6 +812,13 @@ int configure_fft_kernels()
     NUFFT_TRY(allow_fft_smem(k_line4_batch<16>));
     NUFFT_TRY(allow_fft_smem(k_line4_batch<20>));
     NUFFT_TRY(allow_fft_smem(k_line4_batch<24>));
+    NUFFT_TRY(allow_fft_smem(k_fft_batch_p<false>));
+    NUFFT_TRY(allow_fft_smem(k_fft_batch_p<true>));
+    NUFFT_TRY(allow_fft_smem(k_line4_batch_p<8>));
+    NUFFT_TRY(allow_fft_smem(k_line4_batch_p<12>));
+    NUFFT_TRY(allow_fft_smem(k_line4_batch_p<16>));
+    NUFFT_TRY(allow_fft_smem(k_line4_batch_p<20>));
+    NUFFT_TRY(allow_fft_smem(k_line4_batch_p<24>));
     return configure_fft_constants();
 }
 

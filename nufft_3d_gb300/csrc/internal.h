@@ -193,7 +193,20 @@ int line_vec(int64_t rowlen);
 size_t line_smem(int vec, int K);
 bool needs_rare(const FFTDesc &f);
 constexpr int kMaxLineCoilsHost = 16;
+// Descriptors of up to kBatchParamVols volumes of one batched FFT launch,
+// passed by value as the kernel parameter: blocks find their volume by a
+// search over `first` in the parameter bank instead of dependent loads from
+// global memory before they can touch data.
+constexpr int kBatchParamVols = 48;
+struct BatchFFTParams {
+    int nvol;
+    int first[kBatchParamVols + 1];  // first block of each volume; first[nvol] = total
+    int nch[kBatchParamVols];        // coil chunks per line (x passes)
+    BatchFFT v[kBatchParamVols];
+};
+
 int batch_four_step(int K, bool all_vec16);
+int launch_fft_batch_p(const BatchFFTParams &P, int kind, size_t smem, bool rare, int r1, cudaStream_t s);
 size_t batch_four_step_smem(int K);
 int launch_fft_batch4(const BatchFFT *vols, const int4 *table, int nblocks, int r1, cudaStream_t s);
 int launch_fft_batch(const BatchFFT *vols, const int4 *table, int nblocks, int kind, size_t smem, bool rare,
