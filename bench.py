@@ -120,13 +120,22 @@ def stage_bytes(obj, nc):
     }
 
 
-def ncu_traffic(kernel):
-    """DRAM bytes per launch of `kernel` at this workload from the committed ncu summary."""
+def ncu_figures():
     p = os.path.join(ROOT, "profiles", "traffic_config2.json")
     if not os.path.exists(p):
-        return None
+        return {}
     with open(p) as f:
-        return json.load(f).get(kernel)
+        return json.load(f)
+
+
+def ncu_traffic(kernel):
+    """DRAM bytes per launch of `kernel` at this workload from the committed ncu summary."""
+    return ncu_figures().get(kernel)
+
+
+def ncu_sm_side(kernel):
+    """Issue and shared-memory utilisation of `kernel` from the committed ncu summary."""
+    return ncu_figures().get("sm_side", {}).get(kernel)
 
 
 def dist_init():
@@ -408,7 +417,8 @@ def main():
     d = stages[dom]
     roof = {"bound": "hbm", "kernel": dom, "achieved": d["achieved_gbs"], "peak": hbm, "unit": "GB/s",
             "frac": round(d["achieved_gbs"] / hbm, 4), "peak_source": src,
-            "traffic": ncu_traffic(dom), "algo_bytes_per_launch": d["algo_bytes_per_launch"]}
+            "traffic": ncu_traffic(dom), "algo_bytes_per_launch": d["algo_bytes_per_launch"],
+            "sm_side": ncu_sm_side(dom)}
     launches = sum(r["launches"] for r in prof.values())
 
     if rank != 0:
