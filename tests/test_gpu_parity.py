@@ -277,3 +277,21 @@ def test_phase_constraint_matches_oracle(cuda):
     with pytest.warns(UserWarning):
         plain = obj.iNUFT(raw, 1, 0.05, constraint="phase-constraint", lam=0.5, tol=0)
     assert rel(plain, obj.iNUFT(raw, 1, 0.05, tol=0)) < 1e-6
+
+
+@pytest.mark.slow
+def test_config4_grid_cg_matches_oracle(cuda):
+    """Config-4 grid (N=192, K=384^3 four-step FFTs, 16 coils per plan) with a
+    reduced koosh ball (384 x 3000 spokes): 5 CG iterations (tol 0) of coil 0
+    against the FP64 oracle CG on the same density (taken from the plan, so
+    the oracle skips its 20 density sweeps)."""
+    torch = cuda
+    N = 192
+    om = synth.koosh_ball(N, 384, 3000)
+    obj = nufft_3d(om, N, "J", 6)
+    ref = NufftRef(om, N, J=6, d=obj.d.astype(np.float64), matrix=False, workers=os.cpu_count())
+    rng = np.random.default_rng(14)
+    raw = (rng.standard_normal((obj.M, 16)) + 1j * rng.standard_normal((obj.M, 16))).astype(np.complex64)
+    im = img_from_dev(obj.iNUFT(k_to_dev(torch, raw), 5, 1e-3, solver="cg", tol=0))
+    imr = ref.iNUFT(raw[:, :1], 5, 1e-3, solver="cg", tol=0)
+    assert rel(im[..., :1], imr) < TOL_IMG
