@@ -291,6 +291,8 @@ struct nufft3d_plan {
     int64_t n_blocks = 0;
     int coils_per_pass = 8;
     int use_tma = 1;            // bulk tensor copies for interior gather tiles
+    int sm_count = 148;         // multiprocessors of the plan's device
+    int *work = nullptr;        // work counter of the persistent interpolation kernels
     int threads = 256;
     double taps = 0;
     float *U = nullptr;         // deapodization [N1 N2 N3]

@@ -20,6 +20,7 @@
 #include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 #include <mutex>
 
@@ -276,11 +277,25 @@ __device__ __forceinline__ void tma_load_4d(unsigned dst, const CUtensorMap *map
                  : "memory");
 }
 
-// Bounded wait for phase 0 of the barrier; false if it expired.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar)
+// Origin of the padded tile of tile index tid; true if it lies inside the
+// grid on every axis (no wrap-around).
+__device__ __forceinline__ bool tile_origin(const Geom &g, int tid, int &ox, int &oy, int &oz)
+{
+    const int tx = tid % g.nt[0];
+    const int ty = (tid / g.nt[0]) % g.nt[1];
+    const int tz = tid / (g.nt[0] * g.nt[1]);
+    ox = tx * g.T[0] - g.Ra[0];
+    oy = ty * g.T[1] - g.Ra[1];
+    oz = tz * g.T[2] - g.Ra[2];
+    return ox >= 0 && oy >= 0 && oz >= 0 && ox + g.P[0] <= g.K[0] && oy + g.P[1] <= g.K[1] &&
+           oz + g.P[2] <= g.K[2];
+}
+
+// Bounded wait for the phase of the given parity; false if it expired.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity)
 {
     for (int i = 0; i < (1 << 22); ++i)
-        if (mbar_try_wait(bar, 0)) return true;
+        if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
 
@@ -344,56 +359,51 @@ __device__ __forceinline__ void unrotate(float2 (&acc)[CB], int rot)
     }
 }
 
+// One tile piece of the gather: stage the padded tile (bulk tensor copy for
+// interior tiles, completing phase `phase` of the barrier, else per-element
+// asynchronous copies), then interpolate the piece's samples.  Entered and
+// left with the tile free for the next piece (the caller's barrier).
+// Returns false, uniformly over the block, if a bulk copy did not complete.
 template <int CB, bool RADIAL, int R>
-__device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
-                                            const float4 *__restrict__ samples, const int4 bi, const Geom &g,
-                                            const KBParams &kb, float scale, const float *__restrict__ wsample,
-                                            const Cand &cd, float4 *smem4, const CUtensorMap *tmap,
-                                            unsigned long long *bar)
+__device__ __forceinline__ bool gather_piece(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
+                                             const float4 *__restrict__ samples, const int4 bi, const Geom &g,
+                                             const KBParams &kb, float scale, const float *__restrict__ wsample,
+                                             const CandSmem &cs, float2 *tile, const CUtensorMap *tmap,
+                                             unsigned bar_sa, unsigned &phase)
 {
     const int Px = g.P[0];
-    CandSmem cs;
-    float2 *tile = align128(carve_cand(cd, cs, smem4));
-    const int tid = bi.x;
-    const int tx = tid % g.nt[0];
-    const int ty = (tid / g.nt[0]) % g.nt[1];
-    const int tz = tid / (g.nt[0] * g.nt[1]);
-    const int ox = tx * g.T[0] - g.Ra[0], oy = ty * g.T[1] - g.Ra[1], oz = tz * g.T[2] - g.Ra[2];
+    int ox, oy, oz;
+    const bool inside = tile_origin(g, bi.x, ox, oy, oz);
     const int cb = min(CB, nc - c0);
-    const bool bulk = tmap != nullptr && ox >= 0 && oy >= 0 && oz >= 0 && ox + g.P[0] <= g.K[0] &&
-                      oy + g.P[1] <= g.K[1] && oz + g.P[2] <= g.K[2];
-    const unsigned bar_sa = bar ? (unsigned)__cvta_generic_to_shared(bar) : 0u;
+    const bool bulk = tmap != nullptr && inside;
     if (bulk) {
-        if (threadIdx.x == 0) mbar_init(bar_sa, 1);
-        __syncthreads();
         if (threadIdx.x == 0) {
             mbar_expect_tx(bar_sa, (unsigned)(g.P[0] * g.P[1] * g.P[2] * CB * sizeof(float2)));
             tma_load_4d((unsigned)__cvta_generic_to_shared(tile), tmap, 2 * c0, ox, oy, oz, bar_sa);
         }
-    } else
-    // stage the padded tile with asynchronous copies (no register round trip)
-    for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int c, size_t gidx) {
-        float2 *dst = &tile[(size_t)pt * CB + c];
-        if (c < cb) {
-            const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(&G[gidx * nc + c0 + c]) : "memory");
-        } else {
-            *dst = make_float2(0.f, 0.f);
-        }
-    });
-    asm volatile("cp.async.commit_group;" ::: "memory");
-    build_cand(cd, cs);
-    asm volatile("cp.async.wait_all;" ::: "memory");
-    if (bulk) {
-        const bool done = mbar_wait_bounded(bar_sa);
+        const bool done = mbar_wait_bounded(bar_sa, phase);
+        phase ^= 1u;
         if (__syncthreads_or(!done)) {     // block-uniform exit on expiry
             if (threadIdx.x == 0) {
                 atomicOr(&g_interp_err, 1u);
-                mbar_wait_bounded(bar_sa);  // let the copy land before the block exits
+                mbar_wait_bounded(bar_sa, phase ^ 1u);  // let the copy land before the block exits
             }
-            return;
+            return false;
         }
     } else {
+        // stage the padded tile with asynchronous copies (no register round trip)
+        for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int c, size_t gidx) {
+            float2 *dst = &tile[(size_t)pt * CB + c];
+            if (c < cb) {
+                const unsigned sa = (unsigned)__cvta_generic_to_shared(dst);
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(&G[gidx * nc + c0 + c])
+                             : "memory");
+            } else {
+                *dst = make_float2(0.f, 0.f);
+            }
+        });
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_all;" ::: "memory");
         __syncthreads();
     }
     const int lane = threadIdx.x & 31;
@@ -439,19 +449,52 @@ __device__ __forceinline__ void gather_body(const float2 *__restrict__ G, float2
         for (int c = 0; c < CB; ++c)
             if (c % kGroup == lig && c < cb) o[c] = make_float2(acc[c].x * sc_, acc[c].y * sc_);
     }
+    __syncthreads();  // every warp is done with the tile
+    return true;
 }
 
+// Shared set-up of the gather blocks: candidate tables, tile, barrier.
+struct GatherSmem {
+    CandSmem cs;
+    float2 *tile;
+    unsigned bar_sa;
+};
+
+__device__ __forceinline__ GatherSmem gather_setup(const Cand &cd, float4 *smem4, unsigned long long *bar)
+{
+    GatherSmem m;
+    m.tile = align128(carve_cand(cd, m.cs, smem4));
+    m.bar_sa = bar ? (unsigned)__cvta_generic_to_shared(bar) : 0u;
+    build_cand(cd, m.cs);
+    if (bar && threadIdx.x == 0) mbar_init(m.bar_sa, 1);
+    __syncthreads();
+    return m;
+}
+
+// Persistent gather: one block per SM takes tile pieces in order (largest
+// first) from a work counter, so the candidate tables and the barrier are set
+// up once per SM instead of once per piece.
 template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
 k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
-         const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
-         KBParams kb, float scale, const float *__restrict__ wsample, Cand cd,
+         const float4 *__restrict__ samples, const int4 *__restrict__ blocks, int nblocks, int *__restrict__ work,
+         Geom g, KBParams kb, float scale, const float *__restrict__ wsample, Cand cd,
          const __grid_constant__ CUtensorMap tmap, int use_tma)
 {
     extern __shared__ float4 smem4[];
     __shared__ unsigned long long bar;
-    gather_body<CB, RADIAL, R>(G, ks, nc, c0, samples, blocks[blockIdx.x], g, kb, scale, wsample, cd, smem4,
-                               use_tma ? &tmap : nullptr, &bar);
+    __shared__ int next;
+    const GatherSmem m = gather_setup(cd, smem4, &bar);
+    unsigned phase = 0;
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(work, 1);
+        __syncthreads();
+        const int b = next;
+        if (b >= nblocks) break;
+        if (!gather_piece<CB, RADIAL, R>(G, ks, nc, c0, samples, blocks[b], g, kb, scale, wsample, m.cs, m.tile,
+                                         use_tma ? &tmap : nullptr, m.bar_sa, phase))
+            return;
+    }
 }
 
 // Spread: ks -> tile -> grid.  The tile accumulates in 32-bit fixed point
@@ -656,7 +699,17 @@ __global__ void k_permute_out(const float2 *__restrict__ ks, float2 *__restrict_
     const int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (m >= M) return;
     const int s = inv[m];
-    for (int c = 0; c < nc; ++c) {
+    int c = 0;
+    if ((nc & 1) == 0 && s >= 0) {
+        // a sample's coils are one contiguous vector: 16-byte loads of pairs
+        const float4 *src = reinterpret_cast<const float4 *>(ks + (size_t)s * nc);
+        for (; c < nc; c += 2) {
+            const float4 v = src[c >> 1];
+            k[m + M * c] = make_float2(v.x * scale, v.y * scale);
+            k[m + M * (c + 1)] = make_float2(v.z * scale, v.w * scale);
+        }
+    }
+    for (; c < nc; ++c) {
         float2 v = make_float2(0.f, 0.f);
         if (s >= 0) {
             v = ks[(size_t)s * nc + c];
@@ -676,7 +729,16 @@ __global__ void k_permute_in(const float2 *__restrict__ k, float2 *__restrict__ 
     const int s = inv[m];
     if (s < 0) return;
     const float w = wsorted ? wsorted[s] : 1.f;
-    for (int c = 0; c < nc; ++c) {
+    int c = 0;
+    if ((nc & 1) == 0) {
+        // write the sample's contiguous coil vector with 16-byte stores
+        float4 *dst = reinterpret_cast<float4 *>(ks + (size_t)s * nc);
+        for (; c < nc; c += 2) {
+            const float2 a = k[m + M * c], b = k[m + M * (c + 1)];
+            dst[c >> 1] = make_float4(a.x * w, a.y * w, b.x * w, b.y * w);
+        }
+    }
+    for (; c < nc; ++c) {
         float2 v = k[m + M * c];
         ks[(size_t)s * nc + c] = make_float2(v.x * w, v.y * w);
     }
@@ -697,8 +759,10 @@ k_gather_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ ta
     const CUtensorMap *tm = (b.tmap_ok >> lw) & 1 ? &b.tmaps[lw] : nullptr;
     // the kernel weights are evaluated per tap, so they come from the
     // parameter bank (every volume of a batch shares them), not the descriptor
-    gather_body<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, kb, b.scale, b.wsample, cd,
-                               smem4, tm, &bar);
+    const GatherSmem m = gather_setup(cd, smem4, &bar);
+    unsigned phase = 0;
+    gather_piece<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, kb, b.scale, b.wsample,
+                                m.cs, m.tile, tm, m.bar_sa, phase);
 }
 
 template <int CB, bool RADIAL, int R>
@@ -832,8 +896,11 @@ static int gather_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, int c0
     alignas(64) CUtensorMap m;
     std::memset(&m, 0, sizeof(m));
     const int use_tma = p->use_tma && gather_tensor_map<CB>(p, G, nc, &m) ? 1 : 0;
-    k_gather<CB, RADIAL, R><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
-        G, ks, nc, c0, p->samples, p->blocks, p->geom, p->kb, scale, ws, cand_of(p), m, use_tma);
+    NUFFT_CUDA_TRY(cudaMemsetAsync(p->work, 0, sizeof(int), s));
+    const int64_t grid = std::min<int64_t>(p->n_blocks, p->sm_count);
+    k_gather<CB, RADIAL, R><<<(unsigned)grid, kInterpThreads, smem, s>>>(
+        G, ks, nc, c0, p->samples, p->blocks, (int)p->n_blocks, p->work, p->geom, p->kb, scale, ws, cand_of(p), m,
+        use_tma);
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }

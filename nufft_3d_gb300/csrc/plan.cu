@@ -438,6 +438,7 @@ static void free_plan_memory(nufft3d_plan *p)
         for (int a = 0; a < 3; ++a) F(p->tw[a]);
     }
     F(p->wbuf);
+    F(p->work);
     F(p->scratch.B1);
     F(p->scratch.B2);
     if (p->scratch.G != p->scratch.B2) F(p->scratch.G); // 2D: G aliases B2
@@ -743,6 +744,7 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
 
     nufft3d_plan *p = new nufft3d_plan();
     p->device = dev;
+    cudaDeviceGetAttribute(&p->sm_count, cudaDevAttrMultiProcessorCount, dev);
     for (int a = 0; a < 3; ++a) p->N[a] = N[a];
     p->M = M;
     p->J = o.J;
@@ -791,7 +793,8 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
         delete p;
         return fail(NUFFT3D_ERR_CUDA, "cudaStreamCreate failed");
     }
-    int st = build_plan(p, om, o);
+    int st = dmalloc(&p->work, 16, nullptr);  // per handle: handles may run concurrently
+    if (st == NUFFT3D_SUCCESS) st = build_plan(p, om, o);
     if (st != NUFFT3D_SUCCESS) {
         std::string msg = nufft3d_last_error();
         free_plan_memory(p);
@@ -836,6 +839,7 @@ extern "C" int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **out)
     p->cand = src->cand;
     p->n_cand = src->n_cand;
     p->cand_desc = src->cand_desc;
+    p->sm_count = src->sm_count;
     p->coils_per_pass = src->coils_per_pass;
     p->taps = src->taps;
     p->U = src->U;
@@ -851,6 +855,13 @@ extern "C" int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **out)
         p->tables.reset();
         delete p;
         return fail(NUFFT3D_ERR_CUDA, "cudaStreamCreate failed");
+    }
+    if (dmalloc(&p->work, 16, nullptr) != NUFFT3D_SUCCESS) {
+        std::string msg = nufft3d_last_error();
+        cudaStreamDestroy(p->own_stream);
+        p->tables.reset();
+        delete p;
+        return fail(NUFFT3D_ERR_NOMEM, msg);
     }
     *out = p;
     return NUFFT3D_SUCCESS;
