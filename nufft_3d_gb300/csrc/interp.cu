@@ -545,21 +545,18 @@ struct IPlane {
     static constexpr int PS = ((Plane<R>::PS + 29) / 32) * 32 + 2;
 };
 
+// One tile piece of the spread into integer planes that are zero on entry
+// (the flush returns every plane it reads to zero, so a persistent block
+// zeroes its tile only once).  Entered and left with the tile free.
 template <int CB, bool RADIAL, int R>
-__device__ __forceinline__ void spread_body(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
-                                            const float4 *__restrict__ samples, const int4 bi, const Geom &g,
-                                            const KBParams &kb, const Cand &cd, float4 *smem4, float *red,
-                                            TapQueue *queues)
+__device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
+                                             const float4 *__restrict__ samples, const int4 bi, const Geom &g,
+                                             const KBParams &kb, const CandSmem &cs, int *tile, float *red,
+                                             TapQueue *queues)
 {
     constexpr int NP = Lanes<CB>::NP, CPS = Lanes<CB>::CPS;
     constexpr int ps = IPlane<R>::PS;
-    const int Px = g.P[0], PxPy = g.P[0] * g.P[1];
-    CandSmem cs;
-    int *tile = reinterpret_cast<int *>(carve_cand(cd, cs, smem4));
-    const int tid = bi.x;
-    const int tx = tid % g.nt[0];
-    const int ty = (tid / g.nt[0]) % g.nt[1];
-    const int tz = tid / (g.nt[0] * g.nt[1]);
+    const int Px = g.P[0];
     const int cb = min(CB, nc - c0);
     const int send = bi.y + bi.z;
     // scale from the block's largest component
@@ -571,13 +568,8 @@ __device__ __forceinline__ void spread_body(const float2 *__restrict__ ks, float
             m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
         }
     }
-    {   // zero the integer planes with 16-byte stores (ps * CB * 2 is a multiple of 4)
-        int4 *t4 = reinterpret_cast<int4 *>(tile);
-        for (int t = threadIdx.x; t < ps * CB / 2; t += blockDim.x) t4[t] = make_int4(0, 0, 0, 0);
-    }
-    build_cand(cd, cs);
     const float ymax = block_max(m, red);   // contains __syncthreads
-    if (!(ymax > 0.f)) return;             // nothing to add (block-uniform)
+    if (!(ymax > 0.f)) return;             // nothing to add (block-uniform); the tile stays zero
     const float wsum = fmaxf(__int_as_float(bi.w), 1.0f);
     int ey, ecy;
     frexpf(ymax, &ey);                     // ymax < 2^ey
@@ -623,37 +615,69 @@ __device__ __forceinline__ void spread_body(const float2 *__restrict__ ks, float
         }
     }
     __syncthreads();
-    const int ox = tx * g.T[0] - g.Ra[0], oy = ty * g.T[1] - g.Ra[1], oz = tz * g.T[2] - g.Ra[2];
+    int ox, oy, oz;
+    tile_origin(g, bi.x, ox, oy, oz);
     if (CB % 2 == 0 && nc % 2 == 0 && c0 % 2 == 0) {
         for_tile_rows<CB / 2>(g, ox, oy, oz, [&](int pt, int cq, size_t gidx) {
             const int cc = 2 * cq;
             if (cc >= cb) return;
-            const int a = tile[(2 * cc) * ps + pt], b = tile[(2 * cc + 1) * ps + pt];
-            const int e = tile[(2 * cc + 2) * ps + pt], f = tile[(2 * cc + 3) * ps + pt];
+            int *t0 = tile + (size_t)(2 * cc) * ps + pt;
+            const int a = t0[0], b = t0[ps], e = t0[2 * ps], f = t0[3 * ps];
             if ((a | b | e | f) == 0) return;
+            t0[0] = 0;
+            t0[ps] = 0;
+            t0[2 * ps] = 0;
+            t0[3 * ps] = 0;
             atomicAdd(reinterpret_cast<float4 *>(&G[gidx * nc + c0 + cc]),
                       make_float4(a * inv_scale, b * inv_scale, e * inv_scale, f * inv_scale));
         });
     } else {
         for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int cc, size_t gidx) {
             if (cc >= cb) return;
-            const int a = tile[(2 * cc) * ps + pt], b = tile[(2 * cc + 1) * ps + pt];
+            int *t0 = tile + (size_t)(2 * cc) * ps + pt;
+            const int a = t0[0], b = t0[ps];
             if ((a | b) == 0) return;
+            t0[0] = 0;
+            t0[ps] = 0;
             atomicAdd(&G[gidx * nc + c0 + cc], make_float2(a * inv_scale, b * inv_scale));
         });
     }
+    __syncthreads();  // the tile is zero again
 }
 
+template <int R>
+__device__ __forceinline__ int *spread_setup(const Cand &cd, CandSmem &cs, float4 *smem4, int cbk)
+{
+    constexpr int ps = IPlane<R>::PS;
+    int *tile = reinterpret_cast<int *>(carve_cand(cd, cs, smem4));
+    // zero the integer planes once, with 16-byte stores (ps * cbk * 2 is a multiple of 4)
+    int4 *t4 = reinterpret_cast<int4 *>(tile);
+    for (int t = threadIdx.x; t < ps * cbk / 2; t += blockDim.x) t4[t] = make_int4(0, 0, 0, 0);
+    build_cand(cd, cs);
+    __syncthreads();
+    return tile;
+}
+
+// Persistent spread: one block per SM takes tile pieces from a work counter.
 template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
 k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
-         const float4 *__restrict__ samples, const int4 *__restrict__ blocks, Geom g,
-         KBParams kb, Cand cd)
+         const float4 *__restrict__ samples, const int4 *__restrict__ blocks, int nblocks, int *__restrict__ work,
+         Geom g, KBParams kb, Cand cd)
 {
     extern __shared__ float4 smem4[];
     __shared__ float red[33];
     __shared__ TapQueue queues[kInterpThreads / 32];
-    spread_body<CB, RADIAL, R>(ks, G, nc, c0, samples, blocks[blockIdx.x], g, kb, cd, smem4, red, queues);
+    __shared__ int next;
+    CandSmem cs;
+    int *tile = spread_setup<R>(cd, cs, smem4, CB);
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(work, 1);
+        __syncthreads();
+        const int b = next;
+        if (b >= nblocks) break;
+        spread_piece<CB, RADIAL, R>(ks, G, nc, c0, samples, blocks[b], g, kb, cs, tile, red, queues);
+    }
 }
 
 // Plan-time bound for the fixed-point spread: for each block, the largest
@@ -775,7 +799,9 @@ k_spread_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ ta
     const int4 e = table[blockIdx.x];
     const BatchInterp &b = vols[e.x];
     const Cand &cd = b.cand;
-    spread_body<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, kb, cd, smem4, red, queues);
+    CandSmem cs;
+    int *tile = spread_setup<R>(cd, cs, smem4, CB);
+    spread_piece<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, kb, cs, tile, red, queues);
 }
 
 // Batched permutes: block -> (volume, chunk of 256 samples).
@@ -909,8 +935,10 @@ template <int CB, bool RADIAL, int R>
 static int spread_t(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, int c0, cudaStream_t s)
 {
     const size_t smem = (size_t)IPlane<R>::PS * CB * 2 * sizeof(int) + cand_smem_bytes(p->n_cand);
-    k_spread<CB, RADIAL, R><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(
-        ks, G, nc, c0, p->samples, p->blocks, p->geom, p->kb, cand_of(p));
+    NUFFT_CUDA_TRY(cudaMemsetAsync(p->work + 1, 0, sizeof(int), s));
+    const int64_t grid = std::min<int64_t>(p->n_blocks, p->sm_count);
+    k_spread<CB, RADIAL, R><<<(unsigned)grid, kInterpThreads, smem, s>>>(
+        ks, G, nc, c0, p->samples, p->blocks, (int)p->n_blocks, p->work + 1, p->geom, p->kb, cand_of(p));
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }
