@@ -85,3 +85,18 @@ def test_python_class_argument_checks():
         nufft_3d(np.ones((3, 4)), 16, "K", 3)
     with pytest.raises(_lib.NufftError, match="value of u"):
         nufft_3d(np.ones((3, 4)), 16, "u", 9)
+
+
+def test_solver_entry_points_check_arguments_without_a_device():
+    """The warm-start and phase-constrained entry points validate their
+    arguments before touching a device (NULL plan, negative lambda)."""
+    L = _lib.load()
+    buf = (ctypes.c_float * 8)()
+    its = (ctypes.c_int * 1)()
+    for fn in (L.nufft3d_inverse_x0, L.nufft3d_inverse):
+        assert fn(None, buf, buf, 1, 5, 0.1, None, _lib.SOLVER_CG, 0.0, its, None) == _lib.ERR_ARG
+    for fn in (L.nufft3d_inverse_x0_host, L.nufft3d_inverse_host):
+        assert fn(None, buf, buf, 1, 5, 0.1, None, _lib.SOLVER_MINRES, 0.0, its) == _lib.ERR_ARG
+    assert L.nufft3d_inverse_phase(None, buf, buf, 1, 5, 0.1, 0.5, None, 0.0, its, None) == _lib.ERR_ARG
+    assert L.nufft3d_inverse_phase_host(None, buf, buf, 1, 5, 0.1, -1.0, None, 0.0, its) == _lib.ERR_ARG
+    assert "lambda" in _lib.last_error()
