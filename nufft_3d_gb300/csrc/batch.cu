@@ -62,6 +62,7 @@ struct nufft3d_batch {
     BatchInterp *gat = nullptr, *spr = nullptr;
     std::vector<CUtensorMap> h_tmaps;   // [nvol][4] gather maps (coil widths 1, 2, 4, 8)
     CUtensorMap *d_tmaps = nullptr;     // their device copy (start of the descriptor buffer)
+    int *work = nullptr;                // work counter of the persistent interpolation launches
     std::vector<BatchInterp> h_gat, h_spr;
     // interpolation launch groups: one per coil-pass width
     struct IGroup {
@@ -397,7 +398,7 @@ static int run_interp(nufft3d_batch *b, bool gather, cudaStream_t s)
 {
     for (auto &g : b->igroups)
         NUFFT_TRY(launch_interp_batch(gather, g.cb, b->R, b->radial, gather ? b->gat : b->spr, g.tab, g.n, g.smem,
-                                      b->plans[0]->kb, s));
+                                      b->plans[0]->kb, b->work, b->plans[0]->sm_count, s));
     return NUFFT3D_SUCCESS;
 }
 
@@ -643,6 +644,8 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
         return bail(fail(NUFFT3D_ERR_CUDA, "batch event"));
     if (cudaStreamCreateWithFlags(&b->own, cudaStreamNonBlocking) != cudaSuccess)
         return bail(fail(NUFFT3D_ERR_CUDA, "batch stream"));
+    s2 = dalloc(b, &b->work, 16);
+    if (s2 != NUFFT3D_SUCCESS) return bail(s2);
     *out = b;
     return NUFFT3D_SUCCESS;
 }

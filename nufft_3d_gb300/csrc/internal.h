@@ -212,7 +212,7 @@ int launch_fft_batch4(const BatchFFT *vols, const int4 *table, int nblocks, int 
 int launch_fft_batch(const BatchFFT *vols, const int4 *table, int nblocks, int kind, size_t smem, bool rare,
                      cudaStream_t s);
 int launch_interp_batch(bool gather, int cb, int R, bool radial, const BatchInterp *vols, const int4 *table,
-                        int nblocks, size_t smem, const KBParams &kb, cudaStream_t s);
+                        int nblocks, size_t smem, const KBParams &kb, int *work, int nsm, cudaStream_t s);
 int launch_perm_batch(bool out, const BatchPerm *vols, const int4 *table, int nblocks, cudaStream_t s);
 
 // ----------------------------------------------------------------- plan

@@ -768,40 +768,57 @@ __global__ void k_permute_in(const float2 *__restrict__ k, float2 *__restrict__ 
     }
 }
 
-// Batched interpolation: block -> (volume, tile piece, first coil) from
-// `table`; one launch covers every volume of a batch.
+// Batched interpolation, persistent: one block per SM takes (volume, tile
+// piece, first coil) entries of `table` (heaviest first) from a work counter.
+// Every volume of a batch has the same kernel and tile shape, hence the same
+// candidate tables, which are set up once per block.
 template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
-k_gather_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ table, KBParams kb)
+k_gather_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ table, int ntab,
+               int *__restrict__ work, KBParams kb)
 {
     extern __shared__ float4 smem4[];
-    const int4 e = table[blockIdx.x];
-    const BatchInterp &b = vols[e.x];
-    const Cand &cd = b.cand;
     __shared__ unsigned long long bar;
-    constexpr int lw = CB >= 8 ? 3 : CB >= 4 ? 2 : CB >= 2 ? 1 : 0;
-    const CUtensorMap *tm = (b.tmap_ok >> lw) & 1 ? &b.tmaps[lw] : nullptr;
-    // the kernel weights are evaluated per tap, so they come from the
-    // parameter bank (every volume of a batch shares them), not the descriptor
-    const GatherSmem m = gather_setup(cd, smem4, &bar);
+    __shared__ int next;
+    const GatherSmem m = gather_setup(vols[0].cand, smem4, &bar);
     unsigned phase = 0;
-    gather_piece<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, kb, b.scale, b.wsample,
-                                m.cs, m.tile, tm, m.bar_sa, phase);
+    constexpr int lw = CB >= 8 ? 3 : CB >= 4 ? 2 : CB >= 2 ? 1 : 0;
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(work, 1);
+        __syncthreads();
+        const int t = next;
+        if (t >= ntab) break;
+        const int4 e = table[t];
+        const BatchInterp &b = vols[e.x];
+        const CUtensorMap *tm = (b.tmap_ok >> lw) & 1 ? &b.tmaps[lw] : nullptr;
+        // the kernel weights come from the parameter bank (shared by the batch)
+        if (!gather_piece<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, kb, b.scale,
+                                         b.wsample, m.cs, m.tile, tm, m.bar_sa, phase))
+            return;
+    }
 }
 
 template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
-k_spread_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ table, KBParams kb)
+k_spread_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ table, int ntab,
+               int *__restrict__ work, KBParams kb)
 {
     extern __shared__ float4 smem4[];
     __shared__ float red[33];
     __shared__ TapQueue queues[kInterpThreads / 32];
-    const int4 e = table[blockIdx.x];
-    const BatchInterp &b = vols[e.x];
-    const Cand &cd = b.cand;
+    __shared__ int next;
     CandSmem cs;
-    int *tile = spread_setup<R>(cd, cs, smem4, CB);
-    spread_piece<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, kb, cs, tile, red, queues);
+    int *tile = spread_setup<R>(vols[0].cand, cs, smem4, CB);
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(work, 1);
+        __syncthreads();
+        const int t = next;
+        if (t >= ntab) break;
+        const int4 e = table[t];
+        const BatchInterp &b = vols[e.x];
+        spread_piece<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, kb, cs, tile, red,
+                                    queues);
+    }
 }
 
 // Batched permutes: block -> (volume, chunk of 256 samples).
@@ -1042,40 +1059,42 @@ int launch_permute_in(nufft3d_plan *p, const float2 *k, float2 *ks, int nc,
 
 template <int CB, bool RADIAL, int R>
 static int interp_batch_t(bool gather, const BatchInterp *vols, const int4 *table, int nblocks, size_t smem,
-                          const KBParams &kb, cudaStream_t s)
+                          const KBParams &kb, int *work, int nsm, cudaStream_t s)
 {
+    NUFFT_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), s));
+    const int grid = nblocks < nsm ? nblocks : nsm;
     if (gather)
-        k_gather_batch<CB, RADIAL, R><<<nblocks, kInterpThreads, smem, s>>>(vols, table, kb);
+        k_gather_batch<CB, RADIAL, R><<<grid, kInterpThreads, smem, s>>>(vols, table, nblocks, work, kb);
     else
-        k_spread_batch<CB, RADIAL, R><<<nblocks, kInterpThreads, smem, s>>>(vols, table, kb);
+        k_spread_batch<CB, RADIAL, R><<<grid, kInterpThreads, smem, s>>>(vols, table, nblocks, work, kb);
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }
 
 template <int CB, bool RADIAL>
 static int interp_batch_r(bool gather, int R, const BatchInterp *vols, const int4 *table, int nblocks, size_t smem,
-                          const KBParams &kb, cudaStream_t s)
+                          const KBParams &kb, int *work, int nsm, cudaStream_t s)
 {
     switch (R) {
-    case 1: return interp_batch_t<CB, RADIAL, 1>(gather, vols, table, nblocks, smem, kb, s);
-    case 2: return interp_batch_t<CB, RADIAL, 2>(gather, vols, table, nblocks, smem, kb, s);
-    case 3: return interp_batch_t<CB, RADIAL, 3>(gather, vols, table, nblocks, smem, kb, s);
-    default: return interp_batch_t<(CB < 8 ? CB : 4), RADIAL, 4>(gather, vols, table, nblocks, smem, kb, s);
+    case 1: return interp_batch_t<CB, RADIAL, 1>(gather, vols, table, nblocks, smem, kb, work, nsm, s);
+    case 2: return interp_batch_t<CB, RADIAL, 2>(gather, vols, table, nblocks, smem, kb, work, nsm, s);
+    case 3: return interp_batch_t<CB, RADIAL, 3>(gather, vols, table, nblocks, smem, kb, work, nsm, s);
+    default: return interp_batch_t<(CB < 8 ? CB : 4), RADIAL, 4>(gather, vols, table, nblocks, smem, kb, work, nsm, s);
     }
 }
 
 int launch_interp_batch(bool gather, int cb, int R, bool radial, const BatchInterp *vols, const int4 *table,
-                        int nblocks, size_t smem, const KBParams &kb, cudaStream_t s)
+                        int nblocks, size_t smem, const KBParams &kb, int *work, int nsm, cudaStream_t s)
 {
     if (nblocks <= 0) return NUFFT3D_SUCCESS;
-    if (cb >= 8) return radial ? interp_batch_r<8, true>(gather, R, vols, table, nblocks, smem, kb, s)
-                               : interp_batch_r<8, false>(gather, R, vols, table, nblocks, smem, kb, s);
-    if (cb >= 4) return radial ? interp_batch_r<4, true>(gather, R, vols, table, nblocks, smem, kb, s)
-                               : interp_batch_r<4, false>(gather, R, vols, table, nblocks, smem, kb, s);
-    if (cb >= 2) return radial ? interp_batch_r<2, true>(gather, R, vols, table, nblocks, smem, kb, s)
-                               : interp_batch_r<2, false>(gather, R, vols, table, nblocks, smem, kb, s);
-    return radial ? interp_batch_r<1, true>(gather, R, vols, table, nblocks, smem, kb, s)
-                  : interp_batch_r<1, false>(gather, R, vols, table, nblocks, smem, kb, s);
+    if (cb >= 8) return radial ? interp_batch_r<8, true>(gather, R, vols, table, nblocks, smem, kb, work, nsm, s)
+                               : interp_batch_r<8, false>(gather, R, vols, table, nblocks, smem, kb, work, nsm, s);
+    if (cb >= 4) return radial ? interp_batch_r<4, true>(gather, R, vols, table, nblocks, smem, kb, work, nsm, s)
+                               : interp_batch_r<4, false>(gather, R, vols, table, nblocks, smem, kb, work, nsm, s);
+    if (cb >= 2) return radial ? interp_batch_r<2, true>(gather, R, vols, table, nblocks, smem, kb, work, nsm, s)
+                               : interp_batch_r<2, false>(gather, R, vols, table, nblocks, smem, kb, work, nsm, s);
+    return radial ? interp_batch_r<1, true>(gather, R, vols, table, nblocks, smem, kb, work, nsm, s)
+                  : interp_batch_r<1, false>(gather, R, vols, table, nblocks, smem, kb, work, nsm, s);
 }
 
 int launch_perm_batch(bool out, const BatchPerm *vols, const int4 *table, int nblocks, cudaStream_t s)
