@@ -473,7 +473,7 @@ def main():
                        "blocks": obj.n_blocks, "l2": "inputs larger than L2 (grid 1.07 GB), no flush",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "e2e": {"value": round(e2e, 2), "unit": "Msample/s", "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "api": "nufft3d_forward_host + nufft3d_adjoint_host, pinned"},
+                    "d2h_bytes_per_step": d2h, "api": "nufft3d_forward_host + nufft3d_adjoint_host, pinned buffers read/written in place by the kernels"},
             "gpu_launches": launches,
             "roofline": roof,
             "stages": stages,

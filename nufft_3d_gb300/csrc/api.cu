@@ -394,20 +394,51 @@ static int stage_alloc(nufft3d_plan *p, size_t in_bytes, size_t out_bytes)
     return NUFFT3D_SUCCESS;
 }
 
+// Device address of a page-locked host buffer (cudaHostAlloc or
+// cudaHostRegister), through which kernels read or write it directly over the
+// host link; nullptr for pageable memory, which goes through a device staging
+// buffer and cudaMemcpyAsync instead.
+static void *mapped_device_ptr(const void *h)
+{
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
+// Host-pointer operator: page-locked buffers are used in place by the first
+// and last kernels of the chain (the input read once by the x pass or the
+// permute, the output written once), so the transfers ride inside those
+// kernels instead of separate copies; pageable buffers are staged.
+template <typename Op>
+static int host_call(nufft3d_plan *p, const void *in, void *out, size_t bi, size_t bo, Op &&op)
+{
+    cudaStream_t s = p->own_stream;
+    const void *din = mapped_device_ptr(in);
+    void *dout = mapped_device_ptr(out);
+    NUFFT_TRY(stage_alloc(p, din ? 0 : bi, dout ? 0 : bo));
+    if (!din) {
+        NUFFT_CUDA_TRY(cudaMemcpyAsync(p->stage.in, in, bi, cudaMemcpyHostToDevice, s));
+        din = p->stage.in;
+    }
+    NUFFT_TRY(op((const float2 *)din, dout ? (float2 *)dout : (float2 *)p->stage.out, s));
+    if (!dout) NUFFT_CUDA_TRY(cudaMemcpyAsync(out, p->stage.out, bo, cudaMemcpyDeviceToHost, s));
+    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    NUFFT_TRY(interp_check_error());
+    return NUFFT3D_SUCCESS;
+}
+
 extern "C" int nufft3d_forward_host(nufft3d_plan *p, const float *x, float *k, int nc)
 {
     clear_error();
     NUFFT_TRY(check_common(p, x, k, nc));
     DevGuard g(p->device);
     const size_t bi = img_elems(p) * nc * sizeof(float2), bo = (size_t)p->M * nc * sizeof(float2);
-    NUFFT_TRY(stage_alloc(p, bi, bo));
-    cudaStream_t s = p->own_stream;
-    NUFFT_CUDA_TRY(cudaMemcpyAsync(p->stage.in, x, bi, cudaMemcpyHostToDevice, s));
-    NUFFT_TRY(op_forward(p, (const float2 *)p->stage.in, (float2 *)p->stage.out, nc, s));
-    NUFFT_CUDA_TRY(cudaMemcpyAsync(k, p->stage.out, bo, cudaMemcpyDeviceToHost, s));
-    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
-    NUFFT_TRY(interp_check_error());
-    return NUFFT3D_SUCCESS;
+    return host_call(p, x, k, bi, bo, [&](const float2 *din, float2 *dout, cudaStream_t s) {
+        return op_forward(p, din, dout, nc, s);
+    });
 }
 
 extern "C" int nufft3d_adjoint_host(nufft3d_plan *p, const float *k, float *x, int nc)
@@ -416,14 +447,9 @@ extern "C" int nufft3d_adjoint_host(nufft3d_plan *p, const float *k, float *x, i
     NUFFT_TRY(check_common(p, k, x, nc));
     DevGuard g(p->device);
     const size_t bi = (size_t)p->M * nc * sizeof(float2), bo = img_elems(p) * nc * sizeof(float2);
-    NUFFT_TRY(stage_alloc(p, bi, bo));
-    cudaStream_t s = p->own_stream;
-    NUFFT_CUDA_TRY(cudaMemcpyAsync(p->stage.in, k, bi, cudaMemcpyHostToDevice, s));
-    NUFFT_TRY(op_adjoint(p, (const float2 *)p->stage.in, (float2 *)p->stage.out, nc, s));
-    NUFFT_CUDA_TRY(cudaMemcpyAsync(x, p->stage.out, bo, cudaMemcpyDeviceToHost, s));
-    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
-    NUFFT_TRY(interp_check_error());
-    return NUFFT3D_SUCCESS;
+    return host_call(p, k, x, bi, bo, [&](const float2 *din, float2 *dout, cudaStream_t s) {
+        return op_adjoint(p, din, dout, nc, s);
+    });
 }
 
 extern "C" int nufft3d_density(nufft3d_plan *p, int maxit)

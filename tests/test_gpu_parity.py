@@ -295,3 +295,32 @@ def test_config4_grid_cg_matches_oracle(cuda):
     im = img_from_dev(obj.iNUFT(k_to_dev(torch, raw), 5, 1e-3, solver="cg", tol=0))
     imr = ref.iNUFT(raw[:, :1], 5, 1e-3, solver="cg", tol=0)
     assert rel(im[..., :1], imr) < TOL_IMG
+
+
+def test_host_entry_points_pinned_and_pageable_agree(cuda):
+    """nufft3d_forward_host / _adjoint_host read and write page-locked buffers
+    in place (kernels on mapped host memory) and stage pageable ones; both
+    give the device-pointer results."""
+    import ctypes
+    from nufft_3d_gb300 import _lib
+    torch = cuda
+    rng = np.random.default_rng(15)
+    N, M, nc = 32, 20000, 4
+    om = rng.uniform(-N / 2, N / 2 - 1, size=(3, M))
+    obj = nufft_3d(om, N, "J", 6, density_iters=0)
+    L = obj._L
+    x = torch.randn((nc, N, N, N), dtype=torch.complex64)
+    y = torch.randn((nc, M), dtype=torch.complex64)
+    k_dev = obj.fNUFT(x.cuda()).cpu()
+    a_dev = obj.aNUFT(y.cuda()).cpu()
+    for pinned in (True, False):
+        xi = x.pin_memory() if pinned else x.clone()
+        yi = y.pin_memory() if pinned else y.clone()
+        ko = torch.empty((nc, M), dtype=torch.complex64)
+        ao = torch.empty((nc, N, N, N), dtype=torch.complex64)
+        if pinned:
+            ko, ao = ko.pin_memory(), ao.pin_memory()
+        _lib.check(L.nufft3d_forward_host(obj.plan, xi.data_ptr(), ko.data_ptr(), nc))
+        _lib.check(L.nufft3d_adjoint_host(obj.plan, yi.data_ptr(), ao.data_ptr(), nc))
+        assert float((ko - k_dev).abs().max()) == 0.0
+        assert float((ao - a_dev).abs().max()) == 0.0
