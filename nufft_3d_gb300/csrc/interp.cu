@@ -211,8 +211,7 @@ struct Lanes {
 };
 
 struct TapQueue {
-    float w[32];
-    int off[32];
+    int2 e[32];  // (weight bits, tile offset): one 8-byte store and load per tap
 };
 
 // Evaluate candidates [base, base+32) of sample sg; returns the number of hits
@@ -228,8 +227,7 @@ __device__ __forceinline__ int eval_chunk(int base, const SampleGeo &sg, const C
     const unsigned m = __ballot_sync(0xffffffffu, hit);
     if (hit) {
         const int r = __popc(m & ((1u << lane) - 1u));
-        qu.w[r] = w;
-        qu.off[r] = off;
+        qu.e[r] = make_int2(__float_as_int(w), off);
     }
     __syncwarp();
     return __popc(m);
@@ -531,10 +529,11 @@ __device__ __forceinline__ void red_add(int *p, int v)
     asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
 }
 
-// q = round(v) for |v| < 2^22 (exact: the addition rounds to an integer)
-__device__ __forceinline__ int to_fixed(float v)
+// round(a*b) for |a*b| < 2^22 with one fused rounding: the exact product is
+// added to 1.5*2^23, which leaves an integer in the low mantissa bits
+__device__ __forceinline__ int to_fixed_mul(float a, float b)
 {
-    return __float_as_int(v + 12582912.0f) - 0x4B400000;
+    return __float_as_int(fmaf(a, b, 12582912.0f)) - 0x4B400000;
 }
 
 // Integer planes of the spread: one plane per (coil, re/im); the stride is
@@ -602,13 +601,14 @@ __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, floa
         for (int base = 0; base < sg.ln; base += 32) {
             const int nh = eval_chunk<RADIAL>(base, sg, cs, kb, qu, lane);
             for (int t = j; t < nh; t += CPS) {
-                const float w = qu.w[t];
-                const int off = qu.off[t];
-                red_add(pl0 + off, to_fixed(w * y.x));
-                red_add(pl0 + ps + off, to_fixed(w * y.y));
+                const int2 qe = qu.e[t];
+                const float w = __int_as_float(qe.x);
+                const int off = qe.y;
+                red_add(pl0 + off, to_fixed_mul(w, y.x));
+                red_add(pl0 + ps + off, to_fixed_mul(w, y.y));
                 if (CB >= 2) {
-                    red_add(pl0 + 2 * ps + off, to_fixed(w * y.z));
-                    red_add(pl0 + 3 * ps + off, to_fixed(w * y.w));
+                    red_add(pl0 + 2 * ps + off, to_fixed_mul(w, y.z));
+                    red_add(pl0 + 3 * ps + off, to_fixed_mul(w, y.w));
                 }
             }
             __syncwarp();
