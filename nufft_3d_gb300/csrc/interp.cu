@@ -523,10 +523,12 @@ __device__ __forceinline__ float block_max(float v, float *red)
     return red[32];
 }
 
-__device__ __forceinline__ void red_add(int *p, int v)
+// Shared-memory reduction at a 32-bit shared address plus a compile-time
+// byte offset (the planes of one tap differ by constant strides).
+template <int IMM>
+__device__ __forceinline__ void red_add_at(unsigned a, int v)
 {
-    const unsigned a = (unsigned)__cvta_generic_to_shared(p);
-    asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+    asm volatile("red.shared.add.u32 [%0+%2], %1;" ::"r"(a), "r"(v), "n"(IMM) : "memory");
 }
 
 // round(a*b) for |a*b| < 2^22 with one fused rounding: the exact product is
@@ -579,6 +581,7 @@ __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, floa
     const int q = lane / CPS, j = lane % CPS;
     const int c = CB >= 2 ? 2 * q : 0;
     int *pl0 = tile + (size_t)(2 * c) * ps;  // re, im of coil c; then re, im of coil c+1
+    const unsigned pl0_sa = (unsigned)__cvta_generic_to_shared(pl0);
     TapQueue &qu = queues[warp];
     auto load_y = [&](int s, float4 &y) {
         const float2 *src = ks + (size_t)s * nc + c0;
@@ -603,12 +606,12 @@ __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, floa
             for (int t = j; t < nh; t += CPS) {
                 const int2 qe = qu.e[t];
                 const float w = __int_as_float(qe.x);
-                const int off = qe.y;
-                red_add(pl0 + off, to_fixed_mul(w, y.x));
-                red_add(pl0 + ps + off, to_fixed_mul(w, y.y));
+                const unsigned a = pl0_sa + 4u * (unsigned)qe.y;
+                red_add_at<0>(a, to_fixed_mul(w, y.x));
+                red_add_at<4 * ps>(a, to_fixed_mul(w, y.y));
                 if (CB >= 2) {
-                    red_add(pl0 + 2 * ps + off, to_fixed_mul(w, y.z));
-                    red_add(pl0 + 3 * ps + off, to_fixed_mul(w, y.w));
+                    red_add_at<8 * ps>(a, to_fixed_mul(w, y.z));
+                    red_add_at<12 * ps>(a, to_fixed_mul(w, y.w));
                 }
             }
             __syncwarp();
