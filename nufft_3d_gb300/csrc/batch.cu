@@ -46,15 +46,14 @@ struct nufft3d_batch {
     std::vector<nufft3d_plan *> plans;
     std::vector<int> nc;
     // descriptor arrays (device) and their host mirrors
-    BatchFFT *fft[NFFT] = {nullptr};
     std::vector<BatchFFT> h_fft[NFFT];
     // FFT launch groups: volumes with the same FFT length share a launch
     struct FGroup {
-        int4 *tab;
-        int n;
-        size_t smem;
-        int r1 = 0;  // > 0: strided pass by the register four-step FFT (K = 16 r1)
-        std::vector<int> vols;    // volumes of the group, in table order
+        int K = 0;                // transform length of the group
+        size_t smem = 0;          // dynamic shared memory of the Stockham launch
+        bool all_vec16 = true;    // every volume has 16-wide line chunks
+        int r1 = 0;               // > 0: strided pass by the register four-step FFT (K = 16 r1)
+        std::vector<int> vols;    // volumes of the group, in launch order
         std::vector<int> blocks;  // their block counts
         std::vector<int> nch;     // their coil chunks per line (x passes)
     };
@@ -278,17 +277,12 @@ static int64_t fft_blocks(const nufft3d_plan *p, const BatchFFT &d, int stage, i
 
 static int upload(nufft3d_batch *b, cudaStream_t s)
 {
-    // host staging layout: gather tensor maps, fft[0..5], gat, spr, pout, pin
+    // host staging layout: gather tensor maps, gat, spr, pout, pin
     size_t off = 0;
     char *h = static_cast<char *>(b->stage);
     NUFFT_CUDA_TRY(cudaEventSynchronize(b->up_done));  // previous upload has left the staging buffer
     std::memcpy(h, b->h_tmaps.data(), b->h_tmaps.size() * sizeof(CUtensorMap));
     off += b->h_tmaps.size() * sizeof(CUtensorMap);
-    for (int st = 0; st < NFFT; ++st) {
-        const size_t n = b->h_fft[st].size() * sizeof(BatchFFT);
-        std::memcpy(h + off, b->h_fft[st].data(), n);
-        off += n;
-    }
     std::memcpy(h + off, b->h_gat.data(), b->h_gat.size() * sizeof(BatchInterp));
     off += b->h_gat.size() * sizeof(BatchInterp);
     std::memcpy(h + off, b->h_spr.data(), b->h_spr.size() * sizeof(BatchInterp));
@@ -487,60 +481,37 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
         if (needs_rare(plans[v]->fft[0]) || needs_rare(plans[v]->fft[1]) || needs_rare(plans[v]->fft[2]))
             b->rare = true;
     }
-    // descriptors and block tables; FFT launches grouped by transform length
+    // FFT launches grouped by transform length: per group its volumes, their
+    // block counts and coil chunks (descriptors go by value at launch)
     for (int st = 0; st < NFFT; ++st) {
         b->h_fft[st].resize(nvol);
-        std::vector<std::pair<int, std::vector<int4>>> groups;  // (K, table)
-        std::vector<size_t> gsmem;
-        std::vector<char> gvec16;  // every volume of the group has 16-wide line chunks
-        std::vector<std::vector<int>> gvols, gblocks, gnch;
         for (int v = 0; v < nvol; ++v) {
             fill_fft(b, v, &b->h_fft[st][v], st);
             const BatchFFT &d = b->h_fft[st][v];
+            auto &groups = b->fgroups[st];
             size_t gi = 0;
-            while (gi < groups.size() && groups[gi].first != d.fd.n) ++gi;
+            while (gi < groups.size() && groups[gi].K != d.fd.n) ++gi;
             if (gi == groups.size()) {
-                groups.push_back({d.fd.n, {}});
-                gsmem.push_back(0);
-                gvec16.push_back(1);
+                nufft3d_batch::FGroup fg;
+                fg.K = d.fd.n;
+                groups.push_back(fg);
             }
-            if (st != FX && st != IX && d.lp.vec != 16) gvec16[gi] = 0;
-            std::vector<int4> &tab = groups[gi].second;
-            gvols.resize(groups.size());
-            gvols[gi].push_back(v);
+            nufft3d_batch::FGroup &g = groups[gi];
+            g.vols.push_back(v);
             if (st == FX || st == IX) {
                 const int nch = (nc[v] + kMaxLineCoilsHost - 1) / kMaxLineCoilsHost;
-                gblocks.resize(groups.size());
-                gnch.resize(groups.size());
-                gblocks[gi].push_back(d.N23 * nch);
-                gnch[gi].push_back(nch);
-                for (int line = 0; line < d.N23; ++line)
-                    for (int c = 0; c < nch; ++c) tab.push_back(make_int4(v, line, c, 0));
-                gsmem[gi] = std::max(gsmem[gi], line_smem(std::min(nc[v], kMaxLineCoilsHost), d.fd.n));
+                g.blocks.push_back(d.N23 * nch);
+                g.nch.push_back(nch);
+                g.smem = std::max(g.smem, line_smem(std::min(nc[v], kMaxLineCoilsHost), d.fd.n));
             } else {
-                const int64_t nb = fft_blocks(plans[v], d, st, nc[v]);
-                gblocks.resize(groups.size());
-                gnch.resize(groups.size());
-                gblocks[gi].push_back((int)nb);
-                gnch[gi].push_back(1);
-                for (int64_t k = 0; k < nb; ++k) tab.push_back(make_int4(v, (int)k, 0, 0));
-                gsmem[gi] = std::max(gsmem[gi], line_smem(d.lp.vec, d.fd.n));
+                g.blocks.push_back((int)fft_blocks(plans[v], d, st, nc[v]));
+                g.nch.push_back(1);
+                g.smem = std::max(g.smem, line_smem(d.lp.vec, d.fd.n));
+                if (d.lp.vec != 16) g.all_vec16 = false;
             }
         }
-        for (size_t gi = 0; gi < groups.size(); ++gi) {
-            nufft3d_batch::FGroup fg;
-            fg.n = (int)groups[gi].second.size();
-            fg.smem = gsmem[gi];
-            fg.r1 = (st == FX || st == IX) ? 0 : batch_four_step(groups[gi].first, gvec16[gi] != 0);
-            fg.vols = gvols[gi];
-            fg.blocks = gblocks[gi];
-            fg.nch = gnch[gi];
-            int s2 = dalloc(b, &fg.tab, groups[gi].second.size());
-            if (s2 != NUFFT3D_SUCCESS) return bail(s2);
-            if (fg.n && cudaMemcpy(fg.tab, groups[gi].second.data(), fg.n * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess)
-                return bail(fail(NUFFT3D_ERR_CUDA, "batch table upload failed"));
-            b->fgroups[st].push_back(fg);
-        }
+        for (auto &g : b->fgroups[st])
+            g.r1 = (st == FX || st == IX) ? 0 : batch_four_step(g.K, g.all_vec16);
     }
     {
         // interpolation: (volume, piece, first coil), heaviest pieces first
@@ -618,8 +589,7 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
     }
     // one device buffer for all descriptors, mirrored by pinned staging
     b->h_tmaps.assign((size_t)4 * nvol, CUtensorMap{});
-    size_t bytes = 4 * nvol * sizeof(CUtensorMap) + NFFT * nvol * sizeof(BatchFFT) + 2 * nvol * sizeof(BatchInterp) +
-                   2 * nvol * sizeof(BatchPerm);
+    size_t bytes = 4 * nvol * sizeof(CUtensorMap) + 2 * nvol * sizeof(BatchInterp) + 2 * nvol * sizeof(BatchPerm);
     b->stage_bytes = bytes;
     if (cudaMallocHost(&b->stage, bytes) != cudaSuccess) return bail(fail(NUFFT3D_ERR_NOMEM, "batch staging"));
     char *base = nullptr;
@@ -628,10 +598,6 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
     b->dstage = base;
     b->d_tmaps = reinterpret_cast<CUtensorMap *>(base);  // cudaMalloc alignment covers the 64-byte rule
     size_t off = 4 * nvol * sizeof(CUtensorMap);
-    for (int st = 0; st < NFFT; ++st) {
-        b->fft[st] = reinterpret_cast<BatchFFT *>(base + off);
-        off += nvol * sizeof(BatchFFT);
-    }
     b->gat = reinterpret_cast<BatchInterp *>(base + off);
     off += nvol * sizeof(BatchInterp);
     b->spr = reinterpret_cast<BatchInterp *>(base + off);

@@ -331,18 +331,6 @@ k_line4(const float2 *__restrict__ in, float2 *__restrict__ out, LinePass lp, co
     line4_body<R1>(in, out, lp, twg, inv, blockIdx.x, sm);
 }
 
-// Batched strided passes of one transform length: block -> (volume, block)
-template <int R1>
-__global__ void __launch_bounds__(384)
-k_line4_batch(const BatchFFT *__restrict__ vols, const int4 *__restrict__ table)
-{
-    extern __shared__ float2 sm[];
-    const int4 e = table[blockIdx.x];
-    const BatchFFT &b = vols[e.x];
-    const LinePass lp = b.lp;  // in registers: the loops read the strides per element
-    line4_body<R1>(b.in, b.out, lp, b.fd.tw, b.inv, e.y, sm);
-}
-
 static int four_step_r1(int K, int vec)
 {
     if (vec != 16) return 0;
@@ -593,29 +581,6 @@ static int launch_line(const float2 *in, float2 *out, int n_outer, int64_t rowle
     return NUFFT3D_SUCCESS;
 }
 
-// Batched passes over many volumes in one launch: block -> (volume, index,
-// coil chunk) from `table`; kind 0 = x pass forward, 1 = strided pass,
-// 2 = x pass adjoint.
-template <bool RARE>
-__global__ void __launch_bounds__(kFftThreads)
-k_fft_batch(const BatchFFT *__restrict__ vols, const int4 *__restrict__ table, int kind)
-{
-    extern __shared__ float2 sm[];
-    // the volume's descriptor is copied to shared memory once per block: the
-    // FFT passes read its radix list and strides many times, which from
-    // global memory (unlike a kernel parameter) costs a load each time
-    __shared__ BatchFFT d;
-    const int4 e = table[blockIdx.x];
-    if (threadIdx.x == 0) d = vols[e.x];
-    __syncthreads();
-    if (kind == 0)
-        fx_body<RARE>(d.in, d.U, d.out, d.N1, d.N23, d.nc, d.fd, e.y, e.z, sm);
-    else if (kind == 1)
-        line_body<RARE>(d.in, d.out, d.lp, d.fd, d.inv, e.y, sm);
-    else
-        ix_body<RARE>(d.in, d.U, d.out, d.N1, d.N23, d.nc, d.fd, d.scale, d.addend, d.add_coef, e.y, e.z, sm);
-}
-
 __device__ __forceinline__ int batch_volume(const BatchFFTParams &P, int blk)
 {
     int lo = 0, hi = P.nvol - 1;  // largest v with first[v] <= blk
@@ -682,36 +647,6 @@ int launch_fft_batch_p(const BatchFFTParams &P, int kind, size_t smem, bool rare
 // Four-step radix R1 (K = 16 R1) of a strided-pass group whose volumes all
 // have 16-wide line chunks, else 0.
 int batch_four_step(int K, bool all_vec16) { return all_vec16 ? four_step_r1(K, 16) : 0; }
-
-size_t batch_four_step_smem(int K) { return line4_smem(K); }
-
-int launch_fft_batch4(const BatchFFT *vols, const int4 *table, int nblocks, int r1, cudaStream_t s)
-{
-    if (nblocks <= 0) return NUFFT3D_SUCCESS;
-    const int threads = 16 * (r1 > 16 ? r1 : 16);
-    const size_t smem = line4_smem(16 * r1);
-    switch (r1) {
-    case 8: k_line4_batch<8><<<nblocks, threads, smem, s>>>(vols, table); break;
-    case 12: k_line4_batch<12><<<nblocks, threads, smem, s>>>(vols, table); break;
-    case 16: k_line4_batch<16><<<nblocks, threads, smem, s>>>(vols, table); break;
-    case 20: k_line4_batch<20><<<nblocks, threads, smem, s>>>(vols, table); break;
-    default: k_line4_batch<24><<<nblocks, threads, smem, s>>>(vols, table); break;
-    }
-    NUFFT_CUDA_TRY(cudaGetLastError());
-    return NUFFT3D_SUCCESS;
-}
-
-int launch_fft_batch(const BatchFFT *vols, const int4 *table, int nblocks, int kind, size_t smem, bool rare,
-                     cudaStream_t s)
-{
-    if (nblocks <= 0) return NUFFT3D_SUCCESS;
-    if (rare)
-        k_fft_batch<true><<<nblocks, kFftThreads, smem, s>>>(vols, table, kind);
-    else
-        k_fft_batch<false><<<nblocks, kFftThreads, smem, s>>>(vols, table, kind);
-    NUFFT_CUDA_TRY(cudaGetLastError());
-    return NUFFT3D_SUCCESS;
-}
 
 int launch_fx(nufft3d_plan *p, const float2 *img, float2 *B1, int nc, cudaStream_t s)
 {
@@ -800,18 +735,11 @@ int configure_fft_kernels()
     NUFFT_TRY(allow_fft_smem(k_fx<true>));
     NUFFT_TRY(allow_fft_smem(k_ix<true>));
     NUFFT_TRY(allow_fft_smem(k_line<true>));
-    NUFFT_TRY(allow_fft_smem(k_fft_batch<false>));
-    NUFFT_TRY(allow_fft_smem(k_fft_batch<true>));
     NUFFT_TRY(allow_fft_smem(k_line4<8>));
     NUFFT_TRY(allow_fft_smem(k_line4<12>));
     NUFFT_TRY(allow_fft_smem(k_line4<16>));
     NUFFT_TRY(allow_fft_smem(k_line4<20>));
     NUFFT_TRY(allow_fft_smem(k_line4<24>));
-    NUFFT_TRY(allow_fft_smem(k_line4_batch<8>));
-    NUFFT_TRY(allow_fft_smem(k_line4_batch<12>));
-    NUFFT_TRY(allow_fft_smem(k_line4_batch<16>));
-    NUFFT_TRY(allow_fft_smem(k_line4_batch<20>));
-    NUFFT_TRY(allow_fft_smem(k_line4_batch<24>));
     NUFFT_TRY(allow_fft_smem(k_fft_batch_p<false>));
     NUFFT_TRY(allow_fft_smem(k_fft_batch_p<true>));
     NUFFT_TRY(allow_fft_smem(k_line4_batch_p<8>));

@@ -216,10 +216,6 @@ struct BatchFFTParams {
 
 int batch_four_step(int K, bool all_vec16);
 int launch_fft_batch_p(const BatchFFTParams &P, int kind, size_t smem, bool rare, int r1, cudaStream_t s);
-size_t batch_four_step_smem(int K);
-int launch_fft_batch4(const BatchFFT *vols, const int4 *table, int nblocks, int r1, cudaStream_t s);
-int launch_fft_batch(const BatchFFT *vols, const int4 *table, int nblocks, int kind, size_t smem, bool rare,
-                     cudaStream_t s);
 int launch_interp_batch(bool gather, int cb, int R, bool radial, const BatchInterp *vols, const int4 *table,
                         int nblocks, size_t smem, const KBParams &kb, int *work, int nsm, cudaStream_t s);
 int launch_perm_batch(bool out, const BatchPerm *vols, const int4 *table, int nblocks, cudaStream_t s);
