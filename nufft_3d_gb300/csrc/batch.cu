@@ -47,6 +47,7 @@ struct nufft3d_batch {
     std::vector<int> nc;
     // descriptor arrays (device) and their host mirrors
     std::vector<BatchFFT> h_fft[NFFT];
+    std::vector<char> chain;  // per volume: FFT passes as its own chain of launches
     // FFT launch groups: volumes with the same FFT length share a launch
     struct FGroup {
         int K = 0;                // transform length of the group
@@ -363,26 +364,54 @@ static int zero_grids(nufft3d_batch *b, cudaStream_t s)
     return NUFFT3D_SUCCESS;
 }
 
-static int run_fft_stage(nufft3d_batch *b, int st, int kind, cudaStream_t s)
+// FFT passes.  A volume whose x pass fills the GPU on its own (at least 4
+// blocks per SM) runs its chain of passes volume by volume (x -> y -> z, or
+// back), so each intermediate is still in L2 when the next pass reads it;
+// running a stage for all volumes first would evict it.  The smaller volumes
+// share one launch per stage and transform length (descriptors by value as
+// kernel parameters, kBatchParamVols volumes per launch).
+static int run_fft_small(nufft3d_batch *b, int st, int kind, cudaStream_t s)
 {
-    // descriptors go by value as kernel parameters, kBatchParamVols volumes
-    // per launch (current host copies: set_io has filled this call's pointers)
     BatchFFTParams P;
     for (auto &g : b->fgroups[st]) {
-        for (size_t i0 = 0; i0 < g.vols.size(); i0 += kBatchParamVols) {
+        std::vector<size_t> small;
+        for (size_t i = 0; i < g.vols.size(); ++i)
+            if (!b->chain[g.vols[i]]) small.push_back(i);
+        for (size_t i0 = 0; i0 < small.size(); i0 += kBatchParamVols) {
             std::memset(&P, 0, sizeof(P));
-            const size_t i1 = std::min(g.vols.size(), i0 + kBatchParamVols);
+            const size_t i1 = std::min(small.size(), i0 + kBatchParamVols);
             P.nvol = (int)(i1 - i0);
             int acc = 0;
             for (size_t i = i0; i < i1; ++i) {
                 const int j = (int)(i - i0);
                 P.first[j] = acc;
-                P.nch[j] = g.nch[i];
-                P.v[j] = b->h_fft[st][g.vols[i]];
-                acc += g.blocks[i];
+                P.nch[j] = g.nch[small[i]];
+                P.v[j] = b->h_fft[st][g.vols[small[i]]];
+                acc += g.blocks[small[i]];
             }
             P.first[P.nvol] = acc;
             NUFFT_TRY(launch_fft_batch_p(P, kind, g.smem, b->rare, kind == 1 ? g.r1 : 0, s));
+        }
+    }
+    return NUFFT3D_SUCCESS;
+}
+
+static int run_fft_chains(nufft3d_batch *b, bool forward, cudaStream_t s)
+{
+    for (int v = 0; v < b->nvol; ++v) {
+        if (!b->chain[v]) continue;
+        nufft3d_plan *p = b->plans[v];
+        const int nc = b->nc[v];
+        if (forward) {
+            const BatchFFT &x = b->h_fft[FX][v], &y = b->h_fft[FY][v], &z = b->h_fft[FZ][v];
+            NUFFT_TRY(launch_fx(p, x.in, x.out, nc, s));
+            NUFFT_TRY(launch_fy(p, y.in, y.out, nc, s));
+            if (!b->is2d) NUFFT_TRY(launch_fz(p, z.in, z.out, nc, s));
+        } else {
+            const BatchFFT &z = b->h_fft[IZ][v], &y = b->h_fft[IY][v], &x = b->h_fft[IX][v];
+            if (!b->is2d) NUFFT_TRY(launch_iz(p, z.in, z.out, nc, s));
+            NUFFT_TRY(launch_iy(p, y.in, y.out, nc, s));
+            NUFFT_TRY(launch_ix(p, x.in, x.out, nc, x.scale, x.addend, x.add_coef, s));
         }
     }
     return NUFFT3D_SUCCESS;
@@ -398,9 +427,10 @@ static int run_interp(nufft3d_batch *b, bool gather, cudaStream_t s)
 
 static int run_fwd_chain(nufft3d_batch *b, cudaStream_t s)
 {
-    NUFFT_TRY(run_fft_stage(b, FX, 0, s));
-    NUFFT_TRY(run_fft_stage(b, FY, 1, s));
-    if (!b->is2d) NUFFT_TRY(run_fft_stage(b, FZ, 1, s));
+    NUFFT_TRY(run_fft_chains(b, true, s));
+    NUFFT_TRY(run_fft_small(b, FX, 0, s));
+    NUFFT_TRY(run_fft_small(b, FY, 1, s));
+    if (!b->is2d) NUFFT_TRY(run_fft_small(b, FZ, 1, s));
     return run_interp(b, true, s);
 }
 
@@ -408,9 +438,10 @@ static int run_adj_chain(nufft3d_batch *b, cudaStream_t s)
 {
     NUFFT_TRY(zero_grids(b, s));
     NUFFT_TRY(run_interp(b, false, s));
-    if (!b->is2d) NUFFT_TRY(run_fft_stage(b, IZ, 1, s));
-    NUFFT_TRY(run_fft_stage(b, IY, 1, s));
-    return run_fft_stage(b, IX, 2, s);
+    NUFFT_TRY(run_fft_chains(b, false, s));
+    if (!b->is2d) NUFFT_TRY(run_fft_small(b, IZ, 1, s));
+    NUFFT_TRY(run_fft_small(b, IY, 1, s));
+    return run_fft_small(b, IX, 2, s);
 }
 
 static void free_batch(nufft3d_batch *b)
@@ -512,6 +543,11 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
         }
         for (auto &g : b->fgroups[st])
             g.r1 = (st == FX || st == IX) ? 0 : batch_four_step(g.K, g.all_vec16);
+    }
+    b->chain.assign(nvol, 0);
+    for (int v = 0; v < nvol; ++v) {
+        const int nch = (nc[v] + kMaxLineCoilsHost - 1) / kMaxLineCoilsHost;
+        b->chain[v] = (int64_t)b->h_fft[FX][v].N23 * nch >= 4 * (int64_t)plans[v]->sm_count;
     }
     {
         // interpolation: (volume, piece, first coil), heaviest pieces first
