@@ -460,6 +460,13 @@ def main():
             "frac": round(d["achieved_gbs"] / hbm, 4), "peak_source": src,
             "traffic": ncu_traffic(dom), "algo_bytes_per_launch": d["algo_bytes_per_launch"],
             "sm_side": ncu_sm_side(dom)}
+    red = ncu_figures().get("red_shared_u32_peak")
+    if dom == "spread" and red and roof["sm_side"] is not None:
+        # the spread's shared-memory integer reductions against their measured ceiling
+        ops = obj.taps_per_sample * obj.nnz * 2 * nc / (stages["spread"]["ms_per_step"] / 1e3)
+        peak = red["lane_ops_per_clk_per_sm"] * red["sms"] * red["sm_mhz"] * 1e6
+        roof["sm_side"] = dict(roof["sm_side"], red_lane_ops_per_s=round(ops / 1e12, 3), red_peak=round(peak / 1e12, 3),
+                               red_unit="T lane-ops/s", red_frac=round(ops / peak, 3))
     launches = sum(r["launches"] for r in prof.values())
 
     if rank != 0:
