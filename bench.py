@@ -37,7 +37,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "fwd+adj NUFFT Msample/s at 128^3"
-WORKLOAD = "config2: N=128^3, u=2 (K=256^3), J=6 radial KB, koosh ball 256x32768 (M=8388608), 8 coils, complex64"
+WORKLOAD = "koosh ball 256x32768 (M=8388608) at N=128^3, u=2 (K=256^3), J=6 radial KB, 8 coils, complex64"
 
 
 def peaks():
@@ -121,7 +121,7 @@ def stage_bytes(obj, nc):
 
 
 def ncu_figures():
-    p = os.path.join(ROOT, "profiles", "traffic_config2.json")
+    p = os.path.join(ROOT, "profiles", "interp_traffic_N128.json")
     if not os.path.exists(p):
         return {}
     with open(p) as f:
@@ -186,7 +186,7 @@ def rotated(om, seed):
     return R @ om
 
 
-def config3_volumes(n_vol=48, seed=3):
+def uneven_volumes(n_vol=48, seed=3):
     """Batched uneven sizes: N in {64, 96, 128, 160}, radial / stack-of-spirals /
     uniform-random trajectories (0.5-1.5 N^3 samples), 4-16 coils each."""
     from nufft_3d_gb300 import synth
@@ -210,11 +210,11 @@ def config3_volumes(n_vol=48, seed=3):
 
 
 def bench_batched(maxit=20, damp=1e-3):
-    """Config 3: 48 uneven volumes reconstructed by the batched CG (one launch per
+    """48 uneven volumes reconstructed by the batched CG (one launch per
     stage for all volumes) against the same volumes one after another."""
     import torch
     from nufft_3d_gb300 import NufftBatch, nufft_3d
-    vols = config3_volumes()
+    vols = uneven_volumes()
     objs = [nufft_3d(om, N, "J", 6, density_iters=20) for om, N, _, _ in vols]
     ncs = [nc for _, _, nc, _ in vols]
     g = torch.Generator(device="cuda").manual_seed(0)
@@ -237,7 +237,7 @@ def bench_batched(maxit=20, damp=1e-3):
     batch.close()
     for o in objs:
         o.close()
-    return {"workload": "config3: 48 volumes, N in {64,96,128,160}, radial/spiral/random, 4-16 coils, "
+    return {"workload": "48 uneven volumes, N in {64,96,128,160}, radial/spiral/random, 4-16 coils, "
                         "%d CG iterations, damp %g" % (maxit, damp),
             "coil_samples": samples, "batched_volumes_per_s": round(len(vols) / t_b, 3),
             "sequential_volumes_per_s": round(len(vols) / t_s, 3), "speedup": round(t_s / t_b, 3),
@@ -245,8 +245,8 @@ def bench_batched(maxit=20, damp=1e-3):
             "max_rel_l2_batched_vs_single": err}
 
 
-def bench_config4(maxit=50, damp=1e-3):
-    """Config 4: N=192^3 (K=384^3), koosh ball 384 x 60000 (M = 23,040,000), 16
+def bench_large_cg(maxit=50, damp=1e-3):
+    """Large CG: N=192^3 (K=384^3), koosh ball 384 x 60000 (M = 23,040,000), 16
     coils, density from the plan (20 iterations), 50 CG iterations with FP64
     scalars, one CUDA graph per iteration.  Check at this size: coils are
     independent systems, so coils 0-1 solved alone equal the same coils of the
@@ -274,7 +274,7 @@ def bench_config4(maxit=50, damp=1e-3):
     im5 = obj.iNUFT(raw, 5, damp, solver="cg", tol=0)
     im2 = obj.iNUFT(raw[:2].contiguous(), 5, damp, solver="cg", tol=0)
     err = float((im5[:2] - im2).abs().norm() / im2.abs().norm())
-    out = {"workload": "config4: N=192^3 (K=384^3), koosh 384x60000 (M=23040000), 16 coils, density 20 it, "
+    out = {"workload": "large CG: N=192^3 (K=384^3), koosh 384x60000 (M=23040000), 16 coils, density 20 it, "
                        "%d CG iterations, FP64 scalars, one graph per iteration" % maxit,
            "plan_s": round(t_plan, 3), "solve_s": round(t_solve, 3), "iterations": int(max(its)),
            "ms_per_iteration": round(1e3 * t_solve / maxit, 2),
@@ -287,8 +287,8 @@ def bench_config4(maxit=50, damp=1e-3):
 
 
 def serving_requests(n_req=40, rate=20.0, seed=5):
-    """Config 5 stream: Poisson arrivals; 60% reuse one of 8 resident trajectories,
-    40% new ones; shapes from the config-2/3 mixes; 20 CG iterations each."""
+    """Serving stream: Poisson arrivals; 60% reuse one of 8 resident trajectories,
+    40% new ones; N 64-128 koosh balls with 4-8 coils; 20 CG iterations each."""
     from nufft_3d_gb300 import synth
     from nufft_3d_gb300.serving import Request
     rng = np.random.default_rng(seed)
@@ -322,7 +322,7 @@ def bench_serving(slots=4):
               for a, b in zip(served, sorted(plain, key=lambda r: r.arrival)))
     s = summarize(served, wall_s)
     p = summarize(plain, wall_p)
-    return {"workload": "config5: %d requests, Poisson 20 req/s, 60%% on 8 resident trajectories, "
+    return {"workload": "serving: %d requests, Poisson 20 req/s, 60%% on 8 resident trajectories, "
                         "N in {64,96,128}, 4-8 coils, 20 CG iterations" % len(reqs),
             "served": s, "plain": p, "throughput_speedup": round(s["volumes_per_s"] / p["volumes_per_s"], 3),
             "p50_speedup": round(p["p50_ms"] / s["p50_ms"], 3), "slots": slots,
@@ -365,7 +365,7 @@ def main():
     ap.add_argument("--n-spokes", dest="n_spokes", type=int, default=32768)
     ap.add_argument("--nc", type=int, default=8)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-extras", action="store_true", help="skip the batched (config 3) and serving (config 5) runs")
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched, serving and large-CG runs")
     ap.add_argument("--tile", type=str, default=None)
     ap.add_argument("--coils-per-pass", type=int, default=0)
     ap.add_argument("--samples-per-block", type=int, default=0)
@@ -491,7 +491,7 @@ def main():
         torch.cuda.empty_cache()
         line["batched"] = bench_batched()
         line["serving"] = bench_serving()
-        line["config4"] = bench_config4()
+        line["large_cg"] = bench_large_cg()
     if not args.no_cpu_baseline and ws == 1:
         line["cpu_baseline"] = cpu_baseline(om, args.N, args.n_read, nc)
     print(json.dumps(line))

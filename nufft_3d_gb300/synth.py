@@ -1,4 +1,4 @@
-"""Seeded synthetic inputs with the shapes of the reference's demo and configs.
+"""Seeded synthetic inputs with the shapes of the reference's demo and the benchmark workloads.
 
 Nothing here is part of the transform; these build test and benchmark inputs:
 

@@ -96,7 +96,7 @@ def test_random_trajectory_parity(cuda, opts, nc):
     assert rel(a, ref.aNUFT(y)) < TOL_OP
 
 
-def test_config1_plain_method(cuda):
+def test_phantom_N64_plain_method(cuda):
     """N=64 phantom with phase, 64 x 4096 golden-angle koosh ball, J=6, 1 coil:
     fNUFT, aNUFT and 20-iteration CG with damp 1e-3 against the FP64 oracle."""
     torch = cuda
@@ -280,8 +280,8 @@ def test_phase_constraint_matches_oracle(cuda):
 
 
 @pytest.mark.slow
-def test_config4_grid_cg_matches_oracle(cuda):
-    """Config-4 grid (N=192, K=384^3 four-step FFTs, 16 coils per plan) with a
+def test_N192_grid_cg_matches_oracle(cuda):
+    """N=192 grid (K=384^3 four-step FFTs, 16 coils per plan) with a
     reduced koosh ball (384 x 3000 spokes): 5 CG iterations (tol 0) of coil 0
     against the FP64 oracle CG on the same density (taken from the plan, so
     the oracle skips its 20 density sweeps)."""
