@@ -138,7 +138,9 @@ def ncu_sm_side(kernel):
     return ncu_figures().get("sm_side", {}).get(kernel)
 
 
-def dist_init():
+def dist_init(backend="nccl"):
+    """One process per GPU under torchrun (RANK/LOCAL_RANK/WORLD_SIZE/MASTER_*);
+    replicas: ranks share nothing but the barrier and the max-over-ranks time."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
         return 0, 1, 0
@@ -146,8 +148,9 @@ def dist_init():
     import torch.distributed as dist
     rank = int(os.environ["RANK"])
     local = int(os.environ.get("LOCAL_RANK", rank))
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl")
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+    dist.init_process_group(backend)
     return rank, ws, local
 
 
@@ -156,9 +159,17 @@ def max_over_ranks(x, ws):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_throughput(units_per_rank, seconds, ws):
+    """Whole-job rate of independent replicas: all ranks' units over the slowest
+    rank's time (weak scaling: per-rank work fixed)."""
+    t = max_over_ranks(seconds, ws)
+    return units_per_rank * ws / t, t
 
 
 def barrier(ws):
@@ -414,8 +425,9 @@ def main():
     _lib.check(L.nufft3d_profile(plan, 0))
     prof = json.loads(buf.value.decode())
     barrier(ws)
-    ms_max = max_over_ranks(ms, ws)
-    value = M * nc * args.steps * ws / (ms_max / 1e3) / 1e6
+    rate, t_max = replica_throughput(M * nc * args.steps, ms / 1e3, ws)
+    ms_max = t_max * 1e3
+    value = rate / 1e6
 
     # e2e: host-pointer entry points, pinned host buffers, copies inside the timed region
     xh = torch.from_numpy(np.ascontiguousarray(im.transpose(3, 2, 1, 0))).pin_memory()
