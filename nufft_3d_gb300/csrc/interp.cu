@@ -3,12 +3,15 @@
 // The reference builds a sparse matrix H [M x prod(K)] (nufft_3d.m:153-212)
 // and multiplies by H (spmv, nufft_3d.m:259-271) and H' (spmv_t,
 // nufft_3d.m:274-282) through cuSPARSE.  Here the in-bounds samples are
-// sorted by oversampled-grid tile at plan time; one block handles one tile
-// piece: it stages the tile plus a halo of R = ceil(J/2) points in shared
-// memory, evaluates the Kaiser-Bessel weights of kernel.m in registers and
-//   gather: reads the staged grid and writes each sample's value;
-//   spread: accumulates into the staged tile (shared-memory atomics) and adds
-//           the tile to the grid with vector atomics (halos overlap).
+// sorted by oversampled-grid tile at plan time and the tiles split into
+// pieces; persistent blocks (one per SM) take pieces from a work counter,
+// hold the tile plus a halo of R = ceil(J/2) points in shared memory,
+// evaluate the Kaiser-Bessel weights of kernel.m in registers and
+//   gather: read the staged grid (one bulk tensor copy per interior tile) and
+//           write each sample's value;
+//   spread: accumulate into the tile (32-bit fixed-point shared-memory
+//           reductions) and add the tile to the grid with vector atomics
+//           (halos overlap).
 // The neighbour set is the reference's: offsets -R..R around round(u*om),
 // kept when 4*dist2 <= J^2 (radial) or per axis (separable).
 //
@@ -198,12 +201,13 @@ __device__ __forceinline__ void for_tile_rows(const Geom &g, int ox, int oy, int
     }
 }
 
-// Work layout shared by gather and spread: one warp per sample.  All 32
-// lanes evaluate 32 candidate taps at a time (weight + tile offset); the hits
-// are compacted through a per-warp queue and then applied by sub-steps in
-// which lane (q, j) handles queued tap j for coil pair q (NP pairs, CPS taps
-// per sub-step).  Quarter-warps therefore touch 8 neighbouring tile points of
-// one coil plane, which keeps shared-memory accesses free of bank conflicts.
+// Work layout of the spread: one warp per sample.  All 32 lanes evaluate 32
+// candidate taps at a time (weight + tile offset); the hits are compacted
+// through a per-warp queue and then applied by sub-steps in which lane (q, j)
+// handles queued tap j for coil pair q (NP pairs, CPS taps per sub-step).  A
+// quarter-warp adds 8 taps of one coil plane; the candidate order keeps their
+// offsets distinct modulo 8 where it can, so the reductions meet few bank
+// conflicts.  (The gather uses 8 lanes per sample instead, below.)
 template <int CB>
 struct Lanes {
     static constexpr int NP = CB >= 2 ? CB / 2 : 1;  // coil pairs (or one coil)
