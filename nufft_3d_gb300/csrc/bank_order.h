@@ -26,8 +26,10 @@ struct BankOrderStats {
 };
 
 // lo/hi: the box of reflected offsets |f| the list serves (per axis).
+// The first `ncore` entries (the taps inside the support for every f of the
+// box) stay the first ncore entries: swaps never cross that boundary.
 inline void bank_order(std::vector<int> &code, int Px, int PxPy, double J, int radial, int is2d,
-                       const double lo[3], const double hi[3], BankOrderStats *stats = nullptr,
+                       const double lo[3], const double hi[3], int ncore = 0, BankOrderStats *stats = nullptr,
                        int n_samples = 160, int sweeps = 24)
 {
     const int n = (int)code.size();
@@ -116,6 +118,7 @@ inline void bank_order(std::vector<int> &code, int Px, int PxPy, double J, int r
         if (c2 < 0 || c2 >= nchunk || c2 == p1 / 8) continue;
         const int lo = 8 * c2, hi = lo + 8 < n ? lo + 8 : n;
         const int p2 = lo + (int)(uni() * (hi - lo));
+        if ((p1 < ncore) != (p2 < ncore)) continue;
         const int ca = p1 / 8, cb = p2 / 8, ba = p1 / 32, bb = p2 / 32;
         std::swap(pos[p1], pos[p2]);
         const long na = chunk_cost(ca), nb = chunk_cost(cb);

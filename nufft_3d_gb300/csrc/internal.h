@@ -75,26 +75,21 @@ __device__ __forceinline__ float exp_neg(float x)
     return fmaf(e, lo * 0.69314718055994531f, e);
 }
 
-// sum_k c[k] t^k, k = 0..kKBDeg, by Horner's rule; host and device
-// evaluate it with the same fused operations.
-__host__ __device__ __forceinline__ float kb_poly_horner(const float *c, float t)
-{
-    float s = c[kKBDeg];
-#pragma unroll
-    for (int k = kKBDeg - 1; k >= 0; --k) s = fmaf(s, t, c[k]);
-    return s;
-}
-
 __device__ __forceinline__ float kb_weight(float dist2, const KBParams &p)
 {
     // (J/2)^2 - dist2 is exact for dist2 in [(J/2)^2/2, (J/2)^2] (Sterbenz)
     const float t = fmaxf((p.half2 - dist2) * p.inv_half2, 0.0f);
     if (p.poly) {
         // branch-free: a degree-14 polynomial in t interpolating the same
-        // kernel at Chebyshev nodes (max error checked at plan time); Horner
-        // (an Estrin form, shorter dependency chain but more instructions,
-        // measured slower in these issue-bound kernels)
-        return kb_poly_horner(p.c, t);
+        // kernel at Chebyshev nodes (max error checked at plan time with the
+        // same Horner steps); an Estrin form, shorter dependency chain but
+        // more instructions, measured slower in these issue-bound kernels.
+        // Indexed directly (no pointer to the parameter) so the coefficients
+        // stay in the constant bank.
+        float s = p.c[kKBDeg];
+#pragma unroll
+        for (int k = kKBDeg - 1; k >= 0; --k) s = fmaf(s, t, p.c[k]);
+        return s;
     }
     const float y = p.a2_over * t; // (ax/3.75)^2
     if (y < 1.0f) {
@@ -169,6 +164,7 @@ struct Cand {
     int n;          // total entries
     int start[8];   // first entry of sub-cube q's list
     int cnt[8];     // its length
+    int core[8];    // its first core[q] entries are inside the support for every sample of the sub-cube
 };
 
 struct BatchInterp {

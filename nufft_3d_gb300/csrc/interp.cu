@@ -61,7 +61,7 @@ __device__ __forceinline__ int wrap_idx(int x, int K)
 // offset as floats (dx', dy', dz', 0).  The tile offset of a tap is computed
 // from the sample's signed strides, so no per-octant table is needed.
 struct CandSmem {
-    const int *sc;  // [16]: start[8], cnt[8]
+    const int *sc;  // [24]: start[8], cnt[8], core[8]
     float4 *f;      // [n]
 };
 
@@ -70,8 +70,8 @@ struct CandSmem {
 __device__ __forceinline__ float4 *carve_cand(const Cand &cd, CandSmem &cs, float4 *smem4)
 {
     cs.sc = reinterpret_cast<const int *>(smem4);
-    cs.f = smem4 + 4;
-    return smem4 + 4 + cd.n;
+    cs.f = smem4 + 6;
+    return smem4 + 6 + cd.n;
 }
 
 __device__ __forceinline__ void build_cand(const Cand &cd, CandSmem cs)
@@ -80,6 +80,7 @@ __device__ __forceinline__ void build_cand(const Cand &cd, CandSmem cs)
     if (threadIdx.x < 8) {
         sc[threadIdx.x] = cd.start[threadIdx.x];
         sc[8 + threadIdx.x] = cd.cnt[threadIdx.x];
+        sc[16 + threadIdx.x] = cd.core[threadIdx.x];
     }
     for (int i = threadIdx.x; i < cd.n; i += blockDim.x) {
         const int code = cd.list[i];
@@ -88,7 +89,7 @@ __device__ __forceinline__ void build_cand(const Cand &cd, CandSmem cs)
     }
 }
 
-size_t cand_smem_bytes(int n) { return (size_t)(n + 4) * sizeof(float4); }
+size_t cand_smem_bytes(int n) { return (size_t)(n + 6) * sizeof(float4); }
 
 // Per-sample reflected coordinates.
 struct SampleGeo {
@@ -96,6 +97,7 @@ struct SampleGeo {
     float sx, sy, sz;  // signed tile strides of the sample's octant: +-1, +-Px, +-Px*Py
     float b;           // tile index of the rounded position + 1.5*2^23 (see tap)
     int lbase, ln;     // the sample's sub-cube candidate list
+    int lcore;         // its first lcore candidates are inside the support for any f of the sub-cube
 };
 
 // Reads the list starts and lengths from shared memory: call after the
@@ -115,6 +117,7 @@ __device__ __forceinline__ SampleGeo sample_geo(const float4 rec, int Px, int Py
     const int q = (g.fx >= 0.25f ? 1 : 0) | (g.fy >= 0.25f ? 2 : 0) | (g.fz >= 0.25f ? 4 : 0);
     g.lbase = cs.sc[q];
     g.ln = cs.sc[8 + q];
+    g.lcore = cs.sc[16 + q];
     return g;
 }
 
@@ -146,6 +149,22 @@ __device__ __forceinline__ bool tap(int ci, const SampleGeo &g, const CandSmem &
     }
     off = tap_offset(cf, g);
     return true;
+}
+
+// Weight and tile offset of a core candidate (ci < g.lcore: inside the
+// support for every sample of the sub-cube, so there is nothing to test).
+template <bool RADIAL>
+__device__ __forceinline__ void tap_core(int ci, const SampleGeo &g, const CandSmem &cs, const KBParams &kb,
+                                         float &w, int &off)
+{
+    const float4 cf = cs.f[g.lbase + ci];
+    const float ex = cf.x - g.fx, ey = cf.y - g.fy, ez = cf.z - g.fz;
+    const float ex2 = ex * ex, ey2 = ey * ey, ez2 = ez * ez;
+    if (RADIAL)
+        w = kb_weight(ez2 + ey2 + ex2, kb);
+    else
+        w = kb_weight(ez2, kb) * kb_weight(ey2, kb) * kb_weight(ex2, kb);
+    off = tap_offset(cf, g);
 }
 
 // Branch-free form of tap for the hot loops: the candidate index is clamped
@@ -422,11 +441,23 @@ __device__ __forceinline__ bool gather_piece(const float2 *__restrict__ G, float
         const SampleGeo sg = sample_geo(rec_next, Px, g.P[1], cs);
         if (s + ngrp < send) rec_next = __ldg(&samples[s + ngrp]);
         const int niter = (sg.ln + kGroup - 1) / kGroup;
+        const int ncore = sg.lcore / kGroup;  // steps whose 8 candidates are all core
         float2 acc[CB];
 #pragma unroll
         for (int c = 0; c < CB; ++c) acc[c] = make_float2(0.f, 0.f);
-        // two independent candidates per step (ILP)
-        for (int it = 0; it < niter; it += 2) {
+        int it = 0;
+        // core candidates: no support test, two per step (ILP)
+        for (; it + 1 < ncore; it += 2) {
+            const int ci0 = it * kGroup + lig, ci1 = ci0 + kGroup;
+            float w0, w1;
+            int off0, off1;
+            tap_core<RADIAL>(ci0, sg, cs, kb, w0, off0);
+            tap_core<RADIAL>(ci1, sg, cs, kb, w1, off1);
+            accumulate<CB>(acc, tile, off0, w0, ko);
+            accumulate<CB>(acc, tile, off1, w1, ko);
+        }
+        // the rest, two independent candidates per step (ILP)
+        for (; it < niter; it += 2) {
             const int ci0 = it * kGroup + lig, ci1 = ci0 + kGroup;
             float w0, w1;
             int off0, off1;
@@ -480,7 +511,7 @@ template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
 k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
          const float4 *__restrict__ samples, const int4 *__restrict__ blocks, int nblocks, int *__restrict__ work,
-         Geom g, KBParams kb, float scale, const float *__restrict__ wsample, Cand cd,
+         Geom g, KBParams kb, float scale, const float *__restrict__ wsample, const __grid_constant__ Cand cd,
          const __grid_constant__ CUtensorMap tmap, int use_tma)
 {
     extern __shared__ float4 smem4[];
@@ -606,6 +637,8 @@ __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, floa
             load_y(s + nwarps, y_next);
         }
         for (int base = 0; base < sg.ln; base += 32) {
+            // (a core-candidate path without the ballot, as in the gather,
+            // measured slower here)
             const int nh = eval_chunk<RADIAL>(base, sg, cs, kb, qu, lane);
             for (int t = j; t < nh; t += CPS) {
                 const int2 qe = qu.e[t];
@@ -670,7 +703,7 @@ template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
 k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
          const float4 *__restrict__ samples, const int4 *__restrict__ blocks, int nblocks, int *__restrict__ work,
-         Geom g, KBParams kb, Cand cd)
+         Geom g, KBParams kb, const __grid_constant__ Cand cd)
 {
     extern __shared__ float4 smem4[];
     __shared__ float red[33];
@@ -692,7 +725,8 @@ k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
 // atomics; runs once per plan).  Written to blocks[b].w as float bits.
 template <bool RADIAL>
 __global__ void __launch_bounds__(kInterpThreads)
-k_weight_sum(const float4 *__restrict__ samples, int4 *__restrict__ blocks, Geom g, KBParams kb, Cand cd)
+k_weight_sum(const float4 *__restrict__ samples, int4 *__restrict__ blocks, Geom g, KBParams kb,
+             const __grid_constant__ Cand cd)
 {
     extern __shared__ float4 smem4[];
     __shared__ float red[33];

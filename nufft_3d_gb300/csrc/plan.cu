@@ -124,7 +124,8 @@ static void fit_kb_poly(double alpha, double i0a, KBParams &kb)
     double err = 0;
     for (int i = 0; i <= 8192; ++i) {
         const float t = (float)(i / 8192.0);
-        const float s = kb_poly_horner(kb.c, t);
+        float s = kb.c[kKBDeg];  // the device's Horner steps (kb_weight)
+        for (int k = kKBDeg - 1; k >= 0; --k) s = fmaf(s, t, kb.c[k]);
         err = std::max(err, std::fabs((double)s - bessi0_host(alpha * std::sqrt((double)t)) / i0a));
     }
     kb.poly = err < 4e-6 ? 1 : 0;
@@ -202,7 +203,7 @@ static std::vector<double> deap_host(const int N[3], const int K[3], double J, d
 // chunks of 8 for shared-memory banks).  A relative slack of 1e-5 keeps every
 // tap that the single-precision test in the kernels can accept.
 static std::vector<int> make_candidates(int R, int radial, int is2d, double J, const double lo[3],
-                                        const double hi[3])
+                                        const double hi[3], int *ncore)
 {
     const double h2 = (J / 2) * (J / 2) * (1 + 1e-5);
     auto mn = [&](int d, int a) {
@@ -232,6 +233,11 @@ static std::vector<int> make_candidates(int R, int radial, int is2d, double J, c
     std::stable_sort(v.begin(), v.end(), [](const C &a, const C &b) {
         return a.key != b.key ? a.key < b.key : a.key2 < b.key2;
     });
+    // core: inside the support for every f of the box with a margin far above
+    // the single-precision error of the kernels' distance test
+    const double h2core = (J / 2) * (J / 2) * (1 - 1e-4);
+    *ncore = 0;
+    while (*ncore < (int)v.size() && v[*ncore].key <= h2core) ++*ncore;
     std::vector<int> out;
     for (auto &c : v) out.push_back(c.code);
     return out;
@@ -242,7 +248,7 @@ static std::vector<int> make_candidates(int R, int radial, int is2d, double J, c
 // geometry: the ordering search takes a fraction of a second.
 struct CandSet {
     std::vector<int> codes;
-    int start[8], cnt[8];
+    int start[8], cnt[8], core[8];
 };
 
 static const CandSet &candidate_set(int R, int radial, int is2d, double J, int Px, int PxPy)
@@ -262,10 +268,12 @@ static const CandSet &candidate_set(int R, int radial, int is2d, double J, int P
             hi[a] = up ? 0.5 : 0.25;
         }
         if (is2d) lo[2] = hi[2] = 0.0;  // f_z = 0 in 2-D
-        std::vector<int> c = make_candidates(R, radial, is2d, J, lo, hi);
-        bank_order(c, Px, PxPy, J, radial, is2d, lo, hi);
+        int ncore = 0;
+        std::vector<int> c = make_candidates(R, radial, is2d, J, lo, hi, &ncore);
+        bank_order(c, Px, PxPy, J, radial, is2d, lo, hi, ncore);
         cs.start[q] = (int)cs.codes.size();
         cs.cnt[q] = (int)c.size();
+        cs.core[q] = ncore;
         cs.codes.insert(cs.codes.end(), c.begin(), c.end());
     }
     return cache.emplace(key, std::move(cs)).first->second;
@@ -611,6 +619,7 @@ static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts
         for (int q = 0; q < 8; ++q) {
             p->cand_desc.start[q] = cs.start[q];
             p->cand_desc.cnt[q] = cs.cnt[q];
+            p->cand_desc.core[q] = cs.core[q];
         }
     }
     NUFFT_TRY(launch_weight_sum(p, s));
