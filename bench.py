@@ -105,15 +105,17 @@ def stage_bytes(obj, nc):
     c = 8 * nc
     img, u = N1 * N2 * N3, N1 * N2 * N3 * 4
     b1, b2, g = K1 * N2 * N3, K1 * K2 * N3, K1 * K2 * K3
+    # sample records (16 B each) or, with the stored H, its rows (read once per 8-coil pass)
+    h = obj.tap_table_bytes * (nc // 8) if obj.tap_table_bytes and nc >= 8 else nnz * 16
     return {
         "fft_x_fwd": img * c + u + b1 * c,
         "fft_y_fwd": b1 * c + b2 * c,
         "fft_z_fwd": b2 * c + g * c,
-        "gather": g * c + nnz * 16 + nnz * c,
+        "gather": g * c + h + nnz * c,
         "permute_out": nnz * c + M * 4 + M * c,
         "permute_in": M * c + M * 4 + nnz * c,
         "grid_zero": g * c,
-        "spread": nnz * c + nnz * 16 + g * c,
+        "spread": nnz * c + h + g * c,
         "fft_z_adj": g * c + b2 * c,
         "fft_y_adj": b2 * c + b1 * c,
         "fft_x_adj": b1 * c + u + img * c,
@@ -380,6 +382,8 @@ def main():
     ap.add_argument("--tile", type=str, default=None)
     ap.add_argument("--coils-per-pass", type=int, default=0)
     ap.add_argument("--samples-per-block", type=int, default=0)
+    ap.add_argument("--tap-table", dest="tap_table", type=int, default=-1, choices=[-1, 0, 1],
+                    help="stored H: -1 auto (library default), 0 evaluate taps on the fly, 1 always")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -393,7 +397,7 @@ def main():
     om, im = build_inputs(args.N, args.n_read, args.n_spokes, args.nc)
     tile = tuple(int(t) for t in args.tile.split(",")) if args.tile else None
     obj = nufft_3d(om, args.N, "J", 6, "u", 2, device=local, tile=tile, coils_per_pass=args.coils_per_pass,
-                   samples_per_block=args.samples_per_block)
+                   samples_per_block=args.samples_per_block, tap_table=args.tap_table)
     L, plan = obj._L, obj.plan
     nc, M = args.nc, obj.M
     x = torch.from_numpy(np.ascontiguousarray(im.transpose(3, 2, 1, 0))).cuda()
@@ -489,6 +493,7 @@ def main():
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "N": args.N, "M": M, "nnz": obj.nnz, "nc": nc,
                        "taps_per_sample": round(obj.taps_per_sample, 2), "tile": list(obj.tile),
+                       "stored_h_bytes": obj.tap_table_bytes,
                        "blocks": obj.n_blocks, "l2": "inputs larger than L2 (grid 1.07 GB), no flush",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "e2e": {"value": round(e2e, 2), "unit": "Msample/s", "h2d_bytes_per_step": h2d,

@@ -64,6 +64,11 @@ typedef struct nufft3d_opts {
     int max_coils_per_pass; /* coils handled per interpolation pass (0 = auto) */
     int max_samples_per_block; /* samples per interpolation block (0 = auto) */
     int verbose;       /* print the reference's set-up summary to stdout */
+    int tap_table;     /* stored interpolation matrix H (nufft_3d.m:153-212) in
+                          tile order, read by the 8-coil gather passes of fNUFT
+                          (H' is applied on the fly): 1 = build it, 0 = evaluate
+                          the kernel on the fly, -1 = auto (default: build it
+                          when it takes at most half of the free device memory) */
 } nufft3d_opts;
 
 /* Read-only properties (nufft_3d.m:26-43). */
@@ -78,10 +83,12 @@ typedef struct nufft3d_info {
     int64_t n_blocks;  /* interpolation blocks (tile pieces) */
     double taps_per_sample; /* mean nonzeros per row of H */
     int64_t device_bytes;   /* device memory held by the plan (tables + scratch) */
+    int64_t tap_table_bytes; /* part of device_bytes held by the stored H (0 = none) */
 } nufft3d_info;
 
 /* Fills *opts with the reference defaults: J=4, u=2, alpha=0 (Beatty),
- * radial=1, gpu=1, density_iters=20 (nufft_3d.m:27-36, density.m:5). */
+ * radial=1, gpu=1, density_iters=20 (nufft_3d.m:27-36, density.m:5),
+ * tap_table=-1. */
 int nufft3d_opts_default(nufft3d_opts *opts);
 
 /* obj = nufft_3d(om, N, name, value, ...)  -- nufft_3d.m:54-251.

@@ -39,7 +39,8 @@ class Opts(ctypes.Structure):
                 ("radial", ctypes.c_int), ("gpu", ctypes.c_int), ("device", ctypes.c_int),
                 ("d", ctypes.c_void_p), ("density_iters", ctypes.c_int),
                 ("tile", ctypes.c_int * 3), ("max_coils_per_pass", ctypes.c_int),
-                ("max_samples_per_block", ctypes.c_int), ("verbose", ctypes.c_int)]
+                ("max_samples_per_block", ctypes.c_int), ("verbose", ctypes.c_int),
+                ("tap_table", ctypes.c_int)]
 
 
 class Info(ctypes.Structure):
@@ -47,7 +48,7 @@ class Info(ctypes.Structure):
                 ("nnz", ctypes.c_int64), ("J", ctypes.c_double), ("u", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("radial", ctypes.c_int), ("tile", ctypes.c_int * 3),
                 ("n_blocks", ctypes.c_int64), ("taps_per_sample", ctypes.c_double),
-                ("device_bytes", ctypes.c_int64)]
+                ("device_bytes", ctypes.c_int64), ("tap_table_bytes", ctypes.c_int64)]
 
 
 # name -> (restype, argtypes); the exported surface of include/nufft3d.h

@@ -294,6 +294,12 @@ struct nufft3d_plan {
     int use_tma = 1;            // bulk tensor copies for interior gather tiles
     int sm_count = 148;         // multiprocessors of the plan's device
     int *work = nullptr;        // work counter of the persistent interpolation kernels
+    // stored H in tile order (8-coil passes): row of sorted sample s = entries
+    // [8*tap_rows[s], 8*tap_rows[s+1]) of tap_ent, (weight bits, tile offset),
+    // padded with zero weights to whole chunks of 8
+    uint32_t *tap_rows = nullptr;
+    int2 *tap_ent = nullptr;
+    int64_t tap_bytes = 0;
     int threads = 256;
     double taps = 0;
     float *U = nullptr;         // deapodization [N1 N2 N3]
@@ -329,6 +335,12 @@ int launch_gather(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, float sc
                   const float *wsample, cudaStream_t s);
 // plan time: per-block bound on summed weights (blocks[b].w) for the spread
 int launch_weight_sum(nufft3d_plan *p, cudaStream_t s);
+// plan time, stored H: rows[s] = chunks of 8 entries in sample s's row
+int launch_tap_count(nufft3d_plan *p, uint32_t *rows, cudaStream_t s);
+// plan time, stored H: the entries of every row (rows = chunk offsets)
+int launch_tap_fill(nufft3d_plan *p, const uint32_t *rows, int2 *taps, cudaStream_t s);
+// the stored-H kernels serve this plan (8-coil passes, R <= 3)
+bool tap_table_applies(const nufft3d_plan *p);
 // spread: G += H' ks (G zeroed by caller)
 int launch_spread(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, cudaStream_t s);
 // user [M nc] <-> sorted [nnz][nc]

@@ -380,19 +380,15 @@ __device__ __forceinline__ void unrotate(float2 (&acc)[CB], int rot)
     }
 }
 
-// One tile piece of the gather: stage the padded tile (bulk tensor copy for
-// interior tiles, completing phase `phase` of the barrier, else per-element
-// asynchronous copies), then interpolate the piece's samples.  Entered and
-// left with the tile free for the next piece (the caller's barrier).
-// Returns false, uniformly over the block, if a bulk copy did not complete.
-template <int CB, bool RADIAL, int R>
-__device__ __forceinline__ bool gather_piece(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
-                                             const float4 *__restrict__ samples, const int4 bi, const Geom &g,
-                                             const KBParams &kb, float scale, const float *__restrict__ wsample,
-                                             const CandSmem &cs, float2 *tile, const CUtensorMap *tmap,
-                                             unsigned bar_sa, unsigned &phase)
+// Stage the padded tile of piece bi: one bulk tensor copy for interior tiles
+// (completing phase `phase` of the barrier), else per-element asynchronous
+// copies.  Returns false, uniformly over the block, if a bulk copy did not
+// complete; the tile is then not to be read.
+template <int CB>
+__device__ __forceinline__ bool stage_tile(const float2 *__restrict__ G, int nc, int c0, const int4 bi,
+                                           const Geom &g, float2 *tile, const CUtensorMap *tmap, unsigned bar_sa,
+                                           unsigned &phase)
 {
-    const int Px = g.P[0];
     int ox, oy, oz;
     const bool inside = tile_origin(g, bi.x, ox, oy, oz);
     const int cb = min(CB, nc - c0);
@@ -427,6 +423,23 @@ __device__ __forceinline__ bool gather_piece(const float2 *__restrict__ G, float
         asm volatile("cp.async.wait_all;" ::: "memory");
         __syncthreads();
     }
+    return true;
+}
+
+// One tile piece of the gather: stage the padded tile, then interpolate the
+// piece's samples.  Entered and left with the tile free for the next piece
+// (the caller's barrier).  Returns false, uniformly over the block, if a
+// bulk copy did not complete.
+template <int CB, bool RADIAL, int R>
+__device__ __forceinline__ bool gather_piece(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
+                                             const float4 *__restrict__ samples, const int4 bi, const Geom &g,
+                                             const KBParams &kb, float scale, const float *__restrict__ wsample,
+                                             const CandSmem &cs, float2 *tile, const CUtensorMap *tmap,
+                                             unsigned bar_sa, unsigned &phase)
+{
+    if (!stage_tile<CB>(G, nc, c0, bi, g, tile, tmap, bar_sa, phase)) return false;
+    const int Px = g.P[0];
+    const int cb = min(CB, nc - c0);
     const int lane = threadIdx.x & 31;
     const int lig = lane & (kGroup - 1);
     const unsigned gmask = 0xFFu << (lane & ~(kGroup - 1));
@@ -581,6 +594,69 @@ struct IPlane {
     static constexpr int PS = ((Plane<R>::PS + 29) / 32) * 32 + 2;
 };
 
+// Fixed-point scale 2^F of a spread piece from its largest |Re|,|Im| and the
+// plan-time bound on summed weights; false (block-uniform) when the piece
+// adds nothing.  Contains __syncthreads.
+__device__ __forceinline__ bool piece_scale(const float2 *__restrict__ ks, int nc, int c0, int cb, const int4 bi,
+                                            float *red, float &scale, float &inv_scale)
+{
+    const int send = bi.y + bi.z;
+    float m = 0.f;
+    for (int s = bi.y + threadIdx.x; s < send; s += blockDim.x) {
+        const float2 *src = ks + (size_t)s * nc + c0;
+        for (int c = 0; c < cb; ++c) {
+            const float2 v = src[c];
+            m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+        }
+    }
+    const float ymax = block_max(m, red);
+    if (!(ymax > 0.f)) return false;
+    const float wsum = fmaxf(__int_as_float(bi.w), 1.0f);
+    int ey, ecy;
+    frexpf(ymax, &ey);                     // ymax < 2^ey
+    frexpf(ymax * wsum, &ecy);             // wsum*ymax < 2^ecy
+    const int F = min(22 - ey, 30 - ecy);
+    scale = ldexpf(1.f, F);
+    inv_scale = ldexpf(1.f, -F);
+    return true;
+}
+
+// Add the integer planes of piece bi to the grid (vector atomics: the halos
+// of neighbouring tiles overlap) and return every plane read to zero.
+template <int CB, int R>
+__device__ __forceinline__ void flush_tile(float2 *__restrict__ G, int nc, int c0, int cb, const int4 bi,
+                                           const Geom &g, int *tile, float inv_scale)
+{
+    constexpr int ps = IPlane<R>::PS;
+    int ox, oy, oz;
+    tile_origin(g, bi.x, ox, oy, oz);
+    if (CB % 2 == 0 && nc % 2 == 0 && c0 % 2 == 0) {
+        for_tile_rows<CB / 2>(g, ox, oy, oz, [&](int pt, int cq, size_t gidx) {
+            const int cc = 2 * cq;
+            if (cc >= cb) return;
+            int *t0 = tile + (size_t)(2 * cc) * ps + pt;
+            const int a = t0[0], b = t0[ps], e = t0[2 * ps], f = t0[3 * ps];
+            if ((a | b | e | f) == 0) return;
+            t0[0] = 0;
+            t0[ps] = 0;
+            t0[2 * ps] = 0;
+            t0[3 * ps] = 0;
+            atomicAdd(reinterpret_cast<float4 *>(&G[gidx * nc + c0 + cc]),
+                      make_float4(a * inv_scale, b * inv_scale, e * inv_scale, f * inv_scale));
+        });
+    } else {
+        for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int cc, size_t gidx) {
+            if (cc >= cb) return;
+            int *t0 = tile + (size_t)(2 * cc) * ps + pt;
+            const int a = t0[0], b = t0[ps];
+            if ((a | b) == 0) return;
+            t0[0] = 0;
+            t0[ps] = 0;
+            atomicAdd(&G[gidx * nc + c0 + cc], make_float2(a * inv_scale, b * inv_scale));
+        });
+    }
+}
+
 // One tile piece of the spread into integer planes that are zero on entry
 // (the flush returns every plane it reads to zero, so a persistent block
 // zeroes its tile only once).  Entered and left with the tile free.
@@ -595,23 +671,8 @@ __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, floa
     const int Px = g.P[0];
     const int cb = min(CB, nc - c0);
     const int send = bi.y + bi.z;
-    // scale from the block's largest component
-    float m = 0.f;
-    for (int s = bi.y + threadIdx.x; s < send; s += blockDim.x) {
-        const float2 *src = ks + (size_t)s * nc + c0;
-        for (int c = 0; c < cb; ++c) {
-            const float2 v = src[c];
-            m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
-        }
-    }
-    const float ymax = block_max(m, red);   // contains __syncthreads
-    if (!(ymax > 0.f)) return;             // nothing to add (block-uniform); the tile stays zero
-    const float wsum = fmaxf(__int_as_float(bi.w), 1.0f);
-    int ey, ecy;
-    frexpf(ymax, &ey);                     // ymax < 2^ey
-    frexpf(ymax * wsum, &ecy);             // wsum*ymax < 2^ecy
-    const int F = min(22 - ey, 30 - ecy);
-    const float scale = ldexpf(1.f, F), inv_scale = ldexpf(1.f, -F);
+    float scale, inv_scale;
+    if (!piece_scale(ks, nc, c0, cb, bi, red, scale, inv_scale)) return;  // the tile stays zero
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int q = lane / CPS, j = lane % CPS;
     const int c = CB >= 2 ? 2 * q : 0;
@@ -655,33 +716,7 @@ __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, floa
         }
     }
     __syncthreads();
-    int ox, oy, oz;
-    tile_origin(g, bi.x, ox, oy, oz);
-    if (CB % 2 == 0 && nc % 2 == 0 && c0 % 2 == 0) {
-        for_tile_rows<CB / 2>(g, ox, oy, oz, [&](int pt, int cq, size_t gidx) {
-            const int cc = 2 * cq;
-            if (cc >= cb) return;
-            int *t0 = tile + (size_t)(2 * cc) * ps + pt;
-            const int a = t0[0], b = t0[ps], e = t0[2 * ps], f = t0[3 * ps];
-            if ((a | b | e | f) == 0) return;
-            t0[0] = 0;
-            t0[ps] = 0;
-            t0[2 * ps] = 0;
-            t0[3 * ps] = 0;
-            atomicAdd(reinterpret_cast<float4 *>(&G[gidx * nc + c0 + cc]),
-                      make_float4(a * inv_scale, b * inv_scale, e * inv_scale, f * inv_scale));
-        });
-    } else {
-        for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int cc, size_t gidx) {
-            if (cc >= cb) return;
-            int *t0 = tile + (size_t)(2 * cc) * ps + pt;
-            const int a = t0[0], b = t0[ps];
-            if ((a | b) == 0) return;
-            t0[0] = 0;
-            t0[ps] = 0;
-            atomicAdd(&G[gidx * nc + c0 + cc], make_float2(a * inv_scale, b * inv_scale));
-        });
-    }
+    flush_tile<CB, R>(G, nc, c0, cb, bi, g, tile, inv_scale);
     __syncthreads();  // the tile is zero again
 }
 
@@ -754,6 +789,303 @@ k_weight_sum(const float4 *__restrict__ samples, int4 *__restrict__ blocks, Geom
     m = block_max(m, red);
     // small safety margin over the single-precision sums
     if (threadIdx.x == 0) blocks[blockIdx.x].w = __float_as_int(m * 1.001f + 1e-3f);
+}
+
+// ------------------------------------------------------------- stored H
+// The reference keeps H as a sparse matrix (nufft_3d.m:153-212).  Its stored
+// form here follows the tile sort: the row of sorted sample s is a run of
+// (weight bits, tile offset) entries in chunks of 8 taps, padded with zero
+// weights to a whole chunk; the rows of a piece are contiguous, so the gather
+// streams them with plain loads that run ahead of the taps and evaluates no
+// kernel weights.  Inside a row the taps are ordered for the shared-memory
+// banks: round-robin over the residue of the tile offset mod 8, and inside
+// each chunk even offsets before odd ones (gather lanes k and k+4 read one
+// 16-byte column of the point-major tile, conflict-free when their offsets
+// differ in parity: about 0.12 collisions per chunk on J=6 radial rows).
+// The residue order would also keep a chunk's 8 taps on distinct banks of
+// the spread's integer planes (about 1.13 wavefronts per chunk), but a
+// spread that streams H through shared memory measured slower than one that
+// evaluates the kernel (staging H costs as many instructions as the weights
+// it saves), so H' is applied on the fly.  The weights are the on-the-fly
+// kernels' (same candidate lists and kernel).
+
+// Streaming load of one stored-H entry (read once: no L1 allocation).
+__device__ __forceinline__ int2 ld_tap(const int2 *p)
+{
+    int2 v;
+    asm volatile("ld.global.nc.L1::no_allocate.v2.s32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+
+// One tile piece of the gather from the stored H (8 coils per pass).  Each
+// group of 8 lanes takes a contiguous run of the piece's samples, whose rows
+// form one contiguous stream of chunks; lane l of the group applies entry l
+// of every chunk (a whole tap: 8 coils, rotated coil-pair reads as in the
+// on-the-fly gather) and keeps the next 4 chunks' entries in registers, so
+// the loads run ahead across sample boundaries.  At the end of a sample the
+// group reduces its 8 partial sums.
+template <int R>
+__device__ __forceinline__ bool gather_piece_tab(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc,
+                                                 int c0, const int4 bi, const Geom &g, float scale,
+                                                 const float *__restrict__ wsample,
+                                                 const uint32_t *__restrict__ rows, const int2 *__restrict__ taps,
+                                                 float2 *tile, const CUtensorMap *tmap, unsigned bar_sa,
+                                                 unsigned &phase)
+{
+    constexpr int CB = 8;
+    const int lane = threadIdx.x & 31, lig = lane & 7;
+    const int grp = threadIdx.x >> 3, ngrp = blockDim.x >> 3;
+    const unsigned gmask = 0xFFu << (lane & 24);
+    const int s_lo = bi.y + (int)(((long long)bi.z * grp) / ngrp);
+    const int s_hi = bi.y + (int)(((long long)bi.z * (grp + 1)) / ngrp);
+    uint32_t cA = 0, nchk = 0;
+    if (s_lo < s_hi) {
+        cA = __ldg(&rows[s_lo]);
+        nchk = __ldg(&rows[s_hi]) - cA;
+    }
+    const int2 *st = taps + (size_t)cA * 8 + lig;
+    const int2 z2 = make_int2(0, 0);
+    // the first chunks land while the tile does
+    int2 e0 = nchk > 0 ? ld_tap(st) : z2;
+    int2 e1 = nchk > 1 ? ld_tap(st + 8) : z2;
+    int2 e2 = nchk > 2 ? ld_tap(st + 16) : z2;
+    int2 e3 = nchk > 3 ? ld_tap(st + 24) : z2;
+    if (!stage_tile<CB>(G, nc, c0, bi, g, tile, tmap, bar_sa, phase)) return false;
+    const int cb = min(CB, nc - c0);
+    const int rot = lig & 3, rot16 = rot << 4;
+    float2 acc[CB];
+#pragma unroll
+    for (int c = 0; c < CB; ++c) acc[c] = make_float2(0.f, 0.f);
+    int s = s_lo;
+    uint32_t send = s < s_hi ? __ldg(&rows[s + 1]) - cA : 0u;      // chunk where sample s ends
+    uint32_t snext = s + 1 < s_hi ? __ldg(&rows[s + 2]) - cA : 0u;  // and sample s+1
+    // write sample s, move to the next one.  Reduce-scatter over the group:
+    // at each of 3 steps a lane keeps half of its coils (the half named by
+    // one bit of its lane index) and adds the partner's copy of them, so lane
+    // l ends with coil l summed over the 8 lanes (14 shuffles instead of 48).
+    auto finish = [&]() {
+        unrotate<CB>(acc, rot);
+        float2 h4[4], h2[2], h1;
+        const bool b2 = lig & 4, b1 = lig & 2, b0 = lig & 1;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float2 keep = b2 ? acc[4 + k] : acc[k], give = b2 ? acc[k] : acc[4 + k];
+            h4[k].x = keep.x + __shfl_xor_sync(gmask, give.x, 4);
+            h4[k].y = keep.y + __shfl_xor_sync(gmask, give.y, 4);
+        }
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+            const float2 keep = b1 ? h4[2 + k] : h4[k], give = b1 ? h4[k] : h4[2 + k];
+            h2[k].x = keep.x + __shfl_xor_sync(gmask, give.x, 2);
+            h2[k].y = keep.y + __shfl_xor_sync(gmask, give.y, 2);
+        }
+        {
+            const float2 keep = b0 ? h2[1] : h2[0], give = b0 ? h2[0] : h2[1];
+            h1.x = keep.x + __shfl_xor_sync(gmask, give.x, 1);
+            h1.y = keep.y + __shfl_xor_sync(gmask, give.y, 1);
+        }
+        const float sc_ = wsample ? scale * __ldg(&wsample[s]) : scale;
+        if (lig < cb) ks[(size_t)s * nc + c0 + lig] = make_float2(h1.x * sc_, h1.y * sc_);
+#pragma unroll
+        for (int c = 0; c < CB; ++c) acc[c] = make_float2(0.f, 0.f);
+        ++s;
+        send = snext;
+        snext = s + 1 < s_hi ? __ldg(&rows[s + 2]) - cA : 0u;
+    };
+    while (s < s_hi && send == 0u) finish();  // samples without taps
+    auto step = [&](int2 &e, uint32_t ch) {
+        const int2 cur = e;
+        e = ch + 4 < nchk ? ld_tap(st + (size_t)(ch + 4) * 8) : z2;
+        if (cur.x != 0) {
+            // coil pairs in the rotated order rot ^ k (see accumulate)
+            const float w = __int_as_float(cur.x);
+            const char *pb = reinterpret_cast<const char *>(tile) + (size_t)cur.y * (CB * 8);
+#pragma unroll
+            for (int k = 0; k < CB / 2; ++k) {
+                const float4 v = *reinterpret_cast<const float4 *>(pb + (rot16 ^ (k << 4)));
+                acc[2 * k].x = fmaf(w, v.x, acc[2 * k].x);
+                acc[2 * k].y = fmaf(w, v.y, acc[2 * k].y);
+                acc[2 * k + 1].x = fmaf(w, v.z, acc[2 * k + 1].x);
+                acc[2 * k + 1].y = fmaf(w, v.w, acc[2 * k + 1].y);
+            }
+        }
+        if (ch + 1 == send) {
+            finish();
+            while (s < s_hi && send == ch + 1) finish();
+        }
+    };
+    for (uint32_t ch = 0; ch < nchk; ch += 4) {
+        step(e0, ch);
+        if (ch + 1 < nchk) step(e1, ch + 1);
+        if (ch + 2 < nchk) step(e2, ch + 2);
+        if (ch + 3 < nchk) step(e3, ch + 3);
+    }
+    __syncthreads();  // every warp is done with the tile
+    return true;
+}
+
+// Persistent gather from the stored H: shared memory = the tile.
+template <int R>
+__global__ void __launch_bounds__(kInterpThreads)
+k_gather_tab(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
+             const int4 *__restrict__ blocks, int nblocks, int *__restrict__ work, Geom g, float scale,
+             const float *__restrict__ wsample, const uint32_t *__restrict__ rows, const int2 *__restrict__ taps,
+             const __grid_constant__ CUtensorMap tmap, int use_tma)
+{
+    extern __shared__ float4 smem4[];
+    __shared__ unsigned long long bar;
+    __shared__ int next;
+    float2 *tile = align128(smem4);
+    const unsigned bar_sa = (unsigned)__cvta_generic_to_shared(&bar);
+    if (threadIdx.x == 0) mbar_init(bar_sa, 1);
+    __syncthreads();
+    unsigned phase = 0;
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(work, 1);
+        __syncthreads();
+        const int b = next;
+        if (b >= nblocks) break;
+        if (!gather_piece_tab<R>(G, ks, nc, c0, blocks[b], g, scale, wsample, rows, taps, tile,
+                                 use_tma ? &tmap : nullptr, bar_sa, phase))
+            return;
+    }
+}
+
+// Weight and tile offset of candidate ci for the stored H.  The distance is
+// formed with explicitly rounded operations (never contracted into FMAs), so
+// the count and fill passes, compiled separately, take identical support
+// decisions.
+template <bool RADIAL>
+__device__ __forceinline__ bool tap_exact(int ci, const SampleGeo &g, const CandSmem &cs, const KBParams &kb,
+                                          float &w, int &off)
+{
+    const float4 cf = cs.f[g.lbase + ci];
+    const float ex = __fsub_rn(cf.x, g.fx), ey = __fsub_rn(cf.y, g.fy), ez = __fsub_rn(cf.z, g.fz);
+    const float ex2 = __fmul_rn(ex, ex), ey2 = __fmul_rn(ey, ey), ez2 = __fmul_rn(ez, ez);
+    const float h2 = kb.half2;
+    if (RADIAL) {
+        const float d2 = __fadd_rn(__fadd_rn(ez2, ey2), ex2);
+        if (!(d2 <= h2)) return false;
+        w = kb_weight(d2, kb);
+    } else {
+        if (!(ex2 <= h2 && ey2 <= h2 && ez2 <= h2)) return false;
+        w = __fmul_rn(__fmul_rn(kb_weight(ez2, kb), kb_weight(ey2, kb)), kb_weight(ex2, kb));
+    }
+    off = tap_offset(cf, g);
+    return true;
+}
+
+__device__ unsigned g_tap_err;  // set when a fill pass finds more hits than its row holds
+
+// Plan time, pass 1 of the stored H: rows[s] = 8-entry chunks of sample s's
+// row (its hits, rounded up).  One warp per sample.
+template <bool RADIAL>
+__global__ void __launch_bounds__(256)
+k_tap_count(const float4 *__restrict__ samples, int64_t nnz, Geom g, KBParams kb, const __grid_constant__ Cand cd,
+            uint32_t *__restrict__ rows)
+{
+    extern __shared__ float4 smem4[];
+    CandSmem cs;
+    carve_cand(cd, cs, smem4);
+    build_cand(cd, cs);
+    __syncthreads();
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nnz; s += nw) {
+        const SampleGeo sg = sample_geo(__ldg(&samples[s]), g.P[0], g.P[1], cs);
+        int nh = 0;
+        for (int base = 0; base < sg.ln; base += 32) {
+            const int ci = base + lane;
+            float w;
+            int off;
+            const bool hit = ci < sg.ln && tap_exact<RADIAL>(ci, sg, cs, kb, w, off);
+            nh += __popc(__ballot_sync(0xffffffffu, hit));
+        }
+        if (lane == 0) rows[s] = (uint32_t)((nh + 7) >> 3);
+    }
+}
+
+// Plan time, pass 2: the entries of every row in bank order (see above).
+// Per warp two shared buffers of cap entries: the hits in candidate order,
+// then in round-robin residue order.
+template <bool RADIAL>
+__global__ void __launch_bounds__(256)
+k_tap_fill(const float4 *__restrict__ samples, int64_t nnz, Geom g, KBParams kb, const __grid_constant__ Cand cd,
+           const uint32_t *__restrict__ rows, int2 *__restrict__ taps, int cap)
+{
+    extern __shared__ float4 smem4[];
+    CandSmem cs;
+    int2 *bufs = reinterpret_cast<int2 *>(carve_cand(cd, cs, smem4));
+    build_cand(cd, cs);
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    int2 *A = bufs + (size_t)warp * 2 * cap, *B = A + cap;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t s = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nnz; s += nw) {
+        const SampleGeo sg = sample_geo(__ldg(&samples[s]), g.P[0], g.P[1], cs);
+        int nh = 0;
+        for (int base = 0; base < sg.ln; base += 32) {
+            const int ci = base + lane;
+            float w = 0.f;
+            int off = 0;
+            const bool hit = ci < sg.ln && tap_exact<RADIAL>(ci, sg, cs, kb, w, off);
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (hit) A[nh + __popc(m & ((1u << lane) - 1u))] = make_int2(__float_as_int(w), off);
+            nh += __popc(m);
+        }
+        __syncwarp();
+        // the row holds what the count pass found; never write past it
+        const size_t row = (size_t)__ldg(&rows[s]) * 8;
+        const int nfill = (int)((size_t)__ldg(&rows[s + 1]) * 8 - row);
+        if (nh > nfill) {
+            if (lane == 0) atomicOr(&g_tap_err, 1u);
+            nh = nfill;
+        }
+        // hits per residue of the tile offset mod 8
+        int cnt = 0;
+        if (lane < 8)
+            for (int i = 0; i < nh; ++i) cnt += (A[i].y & 7) == lane;
+        int n[8];
+#pragma unroll
+        for (int r = 0; r < 8; ++r) n[r] = __shfl_sync(0xffffffffu, cnt, r);
+        // round-robin order: level k holds the k-th hit of every residue that
+        // has one, the residues with more hits first (they run out last)
+        for (int i = lane; i < nh; i += 32) {
+            const int2 e = A[i];
+            const int r = e.y & 7;
+            int rank = 0;
+            for (int i2 = 0; i2 < i; ++i2) rank += (A[i2].y & 7) == r;
+            int nr = 0;
+#pragma unroll
+            for (int r2 = 0; r2 < 8; ++r2) nr = r2 == r ? n[r2] : nr;
+            int pos = 0;
+#pragma unroll
+            for (int r2 = 0; r2 < 8; ++r2) {
+                const bool before = n[r2] > nr || (n[r2] == nr && r2 < r);
+                pos += min(n[r2], rank) + ((before && n[r2] > rank) ? 1 : 0);
+            }
+            B[pos] = e;
+        }
+        __syncwarp();
+        // inside each chunk: even offsets first, then odd ones; zero padding
+        for (int p = lane; p < nfill; p += 32) {
+            if (p >= nh) {
+                taps[row + p] = make_int2(0, 0);
+                continue;
+            }
+            const int c8 = p & ~7, end = min(c8 + 8, nh);
+            int ev = 0, evb = 0;
+            for (int k = c8; k < end; ++k) {
+                const int even = (B[k].y & 1) == 0;
+                ev += even;
+                evb += (k < p) ? even : 0;
+            }
+            const int2 e = B[p];
+            const int slot = (e.y & 1) ? ev + ((p - c8) - evb) : evb;
+            taps[row + c8 + slot] = e;
+        }
+        __syncwarp();  // A and B are refilled for the next sample
+    }
 }
 
 // user layout [M][nc] (coil-major) <-> sorted [nnz][nc] (coil fastest); the
@@ -1001,6 +1333,37 @@ static int spread_t(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, int c0
     return NUFFT3D_SUCCESS;
 }
 
+bool tap_table_applies(const nufft3d_plan *p) { return p->coils_per_pass == 8 && p->geom.R <= 3; }
+
+template <int R>
+static int gather_tab_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, int c0, float scale,
+                        const float *ws, cudaStream_t s)
+{
+    const size_t smem = smem_plane_bytes(R, 8) + 128;
+    alignas(64) CUtensorMap m;
+    std::memset(&m, 0, sizeof(m));
+    const int use_tma = p->use_tma && gather_tensor_map<8>(p, G, nc, &m) ? 1 : 0;
+    NUFFT_CUDA_TRY(cudaMemsetAsync(p->work, 0, sizeof(int), s));
+    const int64_t grid = std::min<int64_t>(p->n_blocks, p->sm_count);
+    k_gather_tab<R><<<(unsigned)grid, kInterpThreads, smem, s>>>(G, ks, nc, c0, p->blocks, (int)p->n_blocks,
+                                                                 p->work, p->geom, scale, ws, p->tap_rows,
+                                                                 p->tap_ent, m, use_tma);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
+// 8-coil gather passes of a plan with the stored H
+static int gather_tab(nufft3d_plan *p, const float2 *in, float2 *out, int nc, int c0, float scale,
+                      const float *ws, cudaStream_t s)
+{
+    switch (p->geom.R) {
+    case 1: return gather_tab_t<1>(p, in, out, nc, c0, scale, ws, s);
+    case 2: return gather_tab_t<2>(p, in, out, nc, c0, scale, ws, s);
+    case 3: return gather_tab_t<3>(p, in, out, nc, c0, scale, ws, s);
+    default: return fail(NUFFT3D_ERR_UNSUPPORTED, "stored H with R > 3");
+    }
+}
+
 template <bool GATHER, int CB, bool RADIAL>
 static int dispatch_r(nufft3d_plan *p, const float2 *in, float2 *out, int nc, int c0, float scale,
                       const float *ws, cudaStream_t s)
@@ -1042,7 +1405,11 @@ static int interp(nufft3d_plan *p, const float2 *in, float2 *out, int nc, float 
         case 1: st = dispatch<GATHER, 1>(p, in, out, nc, c0, scale, ws, s); break;
         case 2: st = dispatch<GATHER, 2>(p, in, out, nc, c0, scale, ws, s); break;
         case 4: st = dispatch<GATHER, 4>(p, in, out, nc, c0, scale, ws, s); break;
-        default: st = dispatch<GATHER, 8>(p, in, out, nc, c0, scale, ws, s); break;
+        default:
+            // the stored H serves the gather; the spread applies H' on the fly
+            st = GATHER && p->tap_ent ? gather_tab(p, in, out, nc, c0, scale, ws, s)
+                                      : dispatch<GATHER, 8>(p, in, out, nc, c0, scale, ws, s);
+            break;
         }
         if (st != NUFFT3D_SUCCESS) return st;
         if (cb > rem) break;
@@ -1061,6 +1428,41 @@ int launch_weight_sum(nufft3d_plan *p, cudaStream_t s)
         k_weight_sum<false><<<(unsigned)p->n_blocks, kInterpThreads, smem, s>>>(p->samples, p->blocks, p->geom,
                                                                              p->kb, cand_of(p));
     NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
+int launch_tap_count(nufft3d_plan *p, uint32_t *rows, cudaStream_t s)
+{
+    if (p->nnz == 0) return NUFFT3D_SUCCESS;
+    const size_t smem = cand_smem_bytes(p->n_cand);
+    const unsigned nb = (unsigned)std::min<int64_t>((p->nnz + 7) / 8, (int64_t)p->sm_count * 8);
+    if (p->geom.radial)
+        k_tap_count<true><<<nb, 256, smem, s>>>(p->samples, p->nnz, p->geom, p->kb, cand_of(p), rows);
+    else
+        k_tap_count<false><<<nb, 256, smem, s>>>(p->samples, p->nnz, p->geom, p->kb, cand_of(p), rows);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
+int launch_tap_fill(nufft3d_plan *p, const uint32_t *rows, int2 *taps, cudaStream_t s)
+{
+    if (p->nnz == 0) return NUFFT3D_SUCCESS;
+    const unsigned zero = 0;
+    NUFFT_CUDA_TRY(cudaMemcpyToSymbolAsync(g_tap_err, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s));
+    int cap = 0;
+    for (int q = 0; q < 8; ++q) cap = std::max(cap, p->cand_desc.cnt[q]);
+    const size_t smem = cand_smem_bytes(p->n_cand) + (size_t)8 * 2 * cap * sizeof(int2);
+    if (smem > 200 * 1024) return fail(NUFFT3D_ERR_UNSUPPORTED, "candidate lists too long for the stored H");
+    const unsigned nb = (unsigned)std::min<int64_t>((p->nnz + 7) / 8, (int64_t)p->sm_count * 8);
+    if (p->geom.radial)
+        k_tap_fill<true><<<nb, 256, smem, s>>>(p->samples, p->nnz, p->geom, p->kb, cand_of(p), rows, taps, cap);
+    else
+        k_tap_fill<false><<<nb, 256, smem, s>>>(p->samples, p->nnz, p->geom, p->kb, cand_of(p), rows, taps, cap);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    unsigned err = 0;
+    NUFFT_CUDA_TRY(cudaMemcpyFromSymbolAsync(&err, g_tap_err, sizeof(err), 0, cudaMemcpyDeviceToHost, s));
+    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    if (err) return fail(NUFFT3D_ERR_CUDA, "stored H: fill pass disagrees with the count pass");
     return NUFFT3D_SUCCESS;
 }
 
@@ -1189,6 +1591,13 @@ int configure_interp_kernels()
 {
     NUFFT_TRY(allow_smem(k_weight_sum<true>));
     NUFFT_TRY(allow_smem(k_weight_sum<false>));
+    NUFFT_TRY(allow_smem(k_tap_count<true>));
+    NUFFT_TRY(allow_smem(k_tap_count<false>));
+    NUFFT_TRY(allow_smem(k_tap_fill<true>));
+    NUFFT_TRY(allow_smem(k_tap_fill<false>));
+    NUFFT_TRY(allow_smem(k_gather_tab<1>));
+    NUFFT_TRY(allow_smem(k_gather_tab<2>));
+    NUFFT_TRY(allow_smem(k_gather_tab<3>));
     NUFFT_TRY(cfg_cb<1>());
     NUFFT_TRY(cfg_cb<2>());
     NUFFT_TRY(cfg_cb<4>());

@@ -22,6 +22,7 @@
 #include <vector>
 
 #include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
 
 #include "bank_order.h"
 #include "internal.h"
@@ -423,7 +424,7 @@ static void adopt_tables(nufft3d_plan *p)
     auto t = std::make_shared<TableOwner>();
     t->device = p->device;
     t->ptrs = {p->samples, p->perm, p->inv, p->blocks, p->cand, p->U, p->d, p->d_orig,
-               p->tw[0], p->tw[1], p->tw[2]};
+               p->tw[0], p->tw[1], p->tw[2], p->tap_rows, p->tap_ent};
     p->tables = t;
 }
 
@@ -444,6 +445,8 @@ static void free_plan_memory(nufft3d_plan *p)
         F(p->d);
         F(p->d_orig);
         for (int a = 0; a < 3; ++a) F(p->tw[a]);
+        F(p->tap_rows);
+        F(p->tap_ent);
     }
     F(p->wbuf);
     F(p->work);
@@ -485,6 +488,68 @@ static int dmalloc(T **ptr, size_t count, int64_t *acc)
         return fail(NUFFT3D_ERR_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
     }
     if (acc) *acc += (int64_t)(count * sizeof(T));
+    return NUFFT3D_SUCCESS;
+}
+
+// The stored H (nufft_3d.m:153-212) in tile order: count each row's chunks,
+// scan them into row offsets, then fill the rows.  mode 0 = none, 1 = always,
+// -1 = when it takes at most half of the free device memory.
+static int build_tap_table(nufft3d_plan *p, int mode, std::vector<void *> &tmp, cudaStream_t s)
+{
+    if (mode == 0 || p->nnz == 0 || !tap_table_applies(p)) return NUFFT3D_SUCCESS;
+    const int64_t nnz = p->nnz;
+    int maxcnt = 0;
+    for (int q = 0; q < 8; ++q) maxcnt = std::max(maxcnt, p->cand_desc.cnt[q]);
+    if ((uint64_t)nnz * (uint64_t)((maxcnt + 7) / 8) >= 0xffffffffull) {  // row offsets are 32-bit chunk indices
+        if (mode < 0) return NUFFT3D_SUCCESS;
+        return fail(NUFFT3D_ERR_SIZE, "too many samples for the stored H");
+    }
+    uint32_t *cnt = nullptr;
+    NUFFT_TRY(dmalloc(&cnt, (size_t)nnz + 1, nullptr));
+    tmp.push_back(cnt);
+    NUFFT_CUDA_TRY(cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * (nnz + 1), s));
+    NUFFT_TRY(launch_tap_count(p, cnt, s));
+    size_t tb = 0;
+    NUFFT_CUDA_TRY(cub::DeviceScan::ExclusiveSum(nullptr, tb, cnt, cnt, (int)(nnz + 1), s));
+    void *tstore = nullptr;
+    NUFFT_TRY(dmalloc((char **)&tstore, tb ? tb : 1, nullptr));
+    tmp.push_back(tstore);
+    uint32_t *rows = nullptr;
+    NUFFT_TRY(dmalloc(&rows, (size_t)nnz + 1, nullptr));
+    uint32_t total = 0;
+    cudaError_t e = cub::DeviceScan::ExclusiveSum(tstore, tb, cnt, rows, (int)(nnz + 1), s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&total, rows + nnz, sizeof(total), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        cudaFree(rows);
+        return fail(NUFFT3D_ERR_CUDA, std::string("stored H row scan: ") + cudaGetErrorString(e));
+    }
+    const uint64_t entries = (uint64_t)total * 8;
+    const uint64_t bytes = entries * sizeof(int2);
+    if (mode < 0) {
+        size_t fr = 0, to = 0;
+        if (cudaMemGetInfo(&fr, &to) != cudaSuccess || bytes > fr / 2) {
+            cudaGetLastError();
+            cudaFree(rows);
+            return NUFFT3D_SUCCESS;  // evaluate on the fly instead
+        }
+    }
+    int2 *taps = nullptr;
+    const int st = dmalloc(&taps, (size_t)entries, nullptr);
+    if (st != NUFFT3D_SUCCESS) {
+        cudaFree(rows);
+        if (mode < 0) {
+            clear_error();
+            return NUFFT3D_SUCCESS;
+        }
+        return st;
+    }
+    p->tap_rows = rows;
+    p->tap_ent = taps;
+    p->tap_bytes = (int64_t)(bytes + sizeof(uint32_t) * (nnz + 1));
+    p->table_bytes += p->tap_bytes;
+    NUFFT_TRY(launch_tap_fill(p, rows, taps, s));
+    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
     return NUFFT3D_SUCCESS;
 }
 
@@ -623,6 +688,7 @@ static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts
         }
     }
     NUFFT_TRY(launch_weight_sum(p, s));
+    NUFFT_TRY(build_tap_table(p, o.tap_table, tmp.ptrs, s));
     // deapodization (FP64 on the host, stored FP32 like deap.m:100-101)
     {
         std::vector<double> U = deap_host(p->N, g.K, p->J, p->alpha, g.radial, g.is2d);
@@ -696,6 +762,7 @@ extern "C" int nufft3d_opts_default(nufft3d_opts *o)
     o->device = -1;
     o->d = nullptr;
     o->density_iters = 20;
+    o->tap_table = -1;
     return NUFFT3D_SUCCESS;
 }
 
@@ -816,6 +883,8 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
                     N[0], N[1], N[2], K[0], K[1], K[2], o.J, o.u, alpha, p->radial);
         std::printf("  %lld points (out of %lld) are within bounds; %.2f taps/sample; %lld blocks\n",
                     (long long)p->nnz, (long long)M, p->taps, (long long)p->n_blocks);
+        if (p->tap_ent)
+            std::printf("  stored H: %.1f MB\n", (double)p->tap_bytes / 1e6);
     }
     *out = p;
     return NUFFT3D_SUCCESS;
@@ -858,6 +927,9 @@ extern "C" int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **out)
         p->tw[a] = src->tw[a];
         p->fft[a] = src->fft[a];
     }
+    p->tap_rows = src->tap_rows;
+    p->tap_ent = src->tap_ent;
+    p->tap_bytes = src->tap_bytes;
     p->table_bytes = src->table_bytes;
     p->tables = src->tables;
     if (cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -922,6 +994,7 @@ extern "C" int nufft3d_plan_info(const nufft3d_plan *p, nufft3d_info *info)
     info->n_blocks = p->n_blocks;
     info->taps_per_sample = p->taps;
     info->device_bytes = p->table_bytes + (int64_t)p->scratch.bytes;
+    info->tap_table_bytes = p->tap_bytes;
     return NUFFT3D_SUCCESS;
 }
 

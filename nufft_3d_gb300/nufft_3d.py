@@ -42,7 +42,7 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
     """obj = nufft_3d(om, N, name, value, ...)"""
 
     def __init__(self, om, N=None, *varargin, device=None, tile=None, coils_per_pass=None,
-                 samples_per_block=None, density_iters=20, verbose=False, **kw):
+                 samples_per_block=None, density_iters=20, verbose=False, tap_table=None, **kw):
         L = _lib.load()
         # name/value pairs (nufft_3d.m:71-76)
         if len(varargin) % 2:
@@ -91,6 +91,8 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
             opts.max_samples_per_block = int(samples_per_block)
         opts.density_iters = int(density_iters) if density_iters > 0 else -1
         opts.verbose = int(bool(verbose))
+        if tap_table is not None:  # True/1 build, False/0 on the fly, -1 auto (default)
+            opts.tap_table = int(tap_table)
         dbuf = None
         if pairs.get("d") is not None:
             dbuf = np.ascontiguousarray(np.asarray(pairs["d"], dtype=np.float32).reshape(-1))
@@ -116,6 +118,7 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
         self.tile = tuple(info.tile[:])
         self.n_blocks = int(info.n_blocks)
         self.taps_per_sample = info.taps_per_sample
+        self.tap_table_bytes = int(info.tap_table_bytes)  # stored H (0: taps evaluated on the fly)
         self._adjoint = False
         if dbuf is not None and abs(float(np.mean(self.d)) - 1) > 1e-6:
             import warnings
