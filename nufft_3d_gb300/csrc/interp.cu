@@ -342,18 +342,16 @@ __device__ __forceinline__ void accumulate(float2 (&acc)[CB], const float2 *tile
 {
     if constexpr (CB >= 2) {
         const char *pb = reinterpret_cast<const char *>(tile) + (size_t)off * (CB * 8);
+        const float2 ww = make_float2(w, w);
 #pragma unroll
         for (int k = 0; k < CB / 2; ++k) {
             const float4 v = *reinterpret_cast<const float4 *>(pb + ko[k]);
-            acc[2 * k].x = fmaf(w, v.x, acc[2 * k].x);
-            acc[2 * k].y = fmaf(w, v.y, acc[2 * k].y);
-            acc[2 * k + 1].x = fmaf(w, v.z, acc[2 * k + 1].x);
-            acc[2 * k + 1].y = fmaf(w, v.w, acc[2 * k + 1].y);
+            // packed FP32x2 FMAs (one instruction per complex value, same rounding as fmaf)
+            acc[2 * k] = __ffma2_rn(ww, make_float2(v.x, v.y), acc[2 * k]);
+            acc[2 * k + 1] = __ffma2_rn(ww, make_float2(v.z, v.w), acc[2 * k + 1]);
         }
     } else {
-        const float2 v = tile[off];
-        acc[0].x = fmaf(w, v.x, acc[0].x);
-        acc[0].y = fmaf(w, v.y, acc[0].y);
+        acc[0] = __ffma2_rn(make_float2(w, w), tile[off], acc[0]);
     }
 }
 
@@ -580,10 +578,12 @@ __device__ __forceinline__ void red_add_at(unsigned a, int v)
 }
 
 // round(a*b) for |a*b| < 2^22 with one fused rounding: the exact product is
-// added to 1.5*2^23, which leaves an integer in the low mantissa bits
-__device__ __forceinline__ int to_fixed_mul(float a, float b)
+// added to 1.5*2^23, which leaves an integer in the low mantissa bits; two
+// at a time with one packed FP32x2 FMA
+__device__ __forceinline__ int2 to_fixed_mul2(float2 a, float2 b)
 {
-    return __float_as_int(fmaf(a, b, 12582912.0f)) - 0x4B400000;
+    const float2 r = __ffma2_rn(a, b, make_float2(12582912.0f, 12582912.0f));
+    return make_int2(__float_as_int(r.x) - 0x4B400000, __float_as_int(r.y) - 0x4B400000);
 }
 
 // Integer planes of the spread: one plane per (coil, re/im); the stride is
@@ -705,11 +705,14 @@ __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, floa
                 const int2 qe = qu.e[t];
                 const float w = __int_as_float(qe.x);
                 const unsigned a = pl0_sa + 4u * (unsigned)qe.y;
-                red_add_at<0>(a, to_fixed_mul(w, y.x));
-                red_add_at<4 * ps>(a, to_fixed_mul(w, y.y));
+                const float2 ww = make_float2(w, w);
+                const int2 v0 = to_fixed_mul2(ww, make_float2(y.x, y.y));
+                red_add_at<0>(a, v0.x);
+                red_add_at<4 * ps>(a, v0.y);
                 if (CB >= 2) {
-                    red_add_at<8 * ps>(a, to_fixed_mul(w, y.z));
-                    red_add_at<12 * ps>(a, to_fixed_mul(w, y.w));
+                    const int2 v1 = to_fixed_mul2(ww, make_float2(y.z, y.w));
+                    red_add_at<8 * ps>(a, v1.x);
+                    red_add_at<12 * ps>(a, v1.y);
                 }
             }
             __syncwarp();
@@ -822,8 +825,8 @@ __device__ __forceinline__ int2 ld_tap(const int2 *p)
 // form one contiguous stream of chunks; lane l of the group applies entry l
 // of every chunk (a whole tap: 8 coils, rotated coil-pair reads as in the
 // on-the-fly gather) and keeps the next 4 chunks' entries in registers, so
-// the loads run ahead across sample boundaries.  At the end of a sample the
-// group reduces its 8 partial sums.
+// the loads run ahead across sample boundaries (2, 3 or 6 chunks measured
+// slower).  At the end of a sample the group reduces its 8 partial sums.
 template <int R>
 __device__ __forceinline__ bool gather_piece_tab(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc,
                                                  int c0, const int4 bi, const Geom &g, float scale,
@@ -893,20 +896,19 @@ __device__ __forceinline__ bool gather_piece_tab(const float2 *__restrict__ G, f
         snext = s + 1 < s_hi ? __ldg(&rows[s + 2]) - cA : 0u;
     };
     while (s < s_hi && send == 0u) finish();  // samples without taps
-    auto step = [&](int2 &e, uint32_t ch) {
-        const int2 cur = e;
-        e = ch + 4 < nchk ? ld_tap(st + (size_t)(ch + 4) * 8) : z2;
+    auto step = [&](int2 &ed, uint32_t ch) {
+        const int2 cur = ed;
+        ed = ch + 4 < nchk ? ld_tap(st + (size_t)(ch + 4) * 8) : z2;
         if (cur.x != 0) {
             // coil pairs in the rotated order rot ^ k (see accumulate)
             const float w = __int_as_float(cur.x);
+            const float2 ww = make_float2(w, w);
             const char *pb = reinterpret_cast<const char *>(tile) + (size_t)cur.y * (CB * 8);
 #pragma unroll
             for (int k = 0; k < CB / 2; ++k) {
                 const float4 v = *reinterpret_cast<const float4 *>(pb + (rot16 ^ (k << 4)));
-                acc[2 * k].x = fmaf(w, v.x, acc[2 * k].x);
-                acc[2 * k].y = fmaf(w, v.y, acc[2 * k].y);
-                acc[2 * k + 1].x = fmaf(w, v.z, acc[2 * k + 1].x);
-                acc[2 * k + 1].y = fmaf(w, v.w, acc[2 * k + 1].y);
+                acc[2 * k] = __ffma2_rn(ww, make_float2(v.x, v.y), acc[2 * k]);
+                acc[2 * k + 1] = __ffma2_rn(ww, make_float2(v.z, v.w), acc[2 * k + 1]);
             }
         }
         if (ch + 1 == send) {
