@@ -105,8 +105,9 @@ def stage_bytes(obj, nc):
     c = 8 * nc
     img, u = N1 * N2 * N3, N1 * N2 * N3 * 4
     b1, b2, g = K1 * N2 * N3, K1 * K2 * N3, K1 * K2 * K3
-    # sample records (16 B each) or, with the stored H, its rows (read once per 8-coil pass)
-    h = obj.tap_table_bytes * (nc // 8) if obj.tap_table_bytes and nc >= 8 else nnz * 16
+    # sample records (16 B each); the gather's 8-coil passes read the stored H's rows instead
+    rec = nnz * 16
+    h = obj.tap_table_bytes * (nc // 8) + rec * (nc % 8 > 0) if obj.tap_table_bytes and nc >= 8 else rec
     return {
         "fft_x_fwd": img * c + u + b1 * c,
         "fft_y_fwd": b1 * c + b2 * c,
@@ -115,7 +116,7 @@ def stage_bytes(obj, nc):
         "permute_out": nnz * c + M * 4 + M * c,
         "permute_in": M * c + M * 4 + nnz * c,
         "grid_zero": g * c,
-        "spread": nnz * c + h + g * c,
+        "spread": nnz * c + rec + g * c,
         "fft_z_adj": g * c + b2 * c,
         "fft_y_adj": b2 * c + b1 * c,
         "fft_x_adj": b1 * c + u + img * c,
