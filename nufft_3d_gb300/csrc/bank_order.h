@@ -5,9 +5,9 @@
 // consecutive candidates is read by 8 lanes in rotated coil-pair order (lanes
 // l and l+4 share the rotation), which is conflict-free when those two taps
 // have tile offsets of different parity.  In the spread 8 consecutive entries
-// of the compacted hit queue are added by one instruction, conflict-free when
-// their offsets differ modulo 8 (the integer planes are shifted by 8 banks per
-// coil pair).  The
+// of the hit queue (the hits of a block of 64 candidates, in list order) are
+// added by one instruction, conflict-free when their offsets differ modulo 8
+// (the integer planes are shifted by 8 banks per coil pair).  The
 // distance-sorted candidate list is therefore re-partitioned by a seeded local
 // search: swaps between nearby chunks (keeping the near-to-far order that
 // lets whole chunks of far taps go idle) are kept by simulated annealing on
@@ -67,7 +67,8 @@ inline void bank_order(std::vector<int> &code, int Px, int PxPy, double J, int r
     }
     std::vector<int> pos(n);  // position -> candidate
     for (int i = 0; i < n; ++i) pos[i] = i;
-    const int nchunk = (n + 7) / 8, nblock = (n + 31) / 32;
+    constexpr int kQ = 64;  // candidates evaluated per spread queue fill
+    const int nchunk = (n + 7) / 8, nblock = (n + kQ - 1) / kQ;
     // gather: lanes l and l+4 of a chunk read the same rotated coil pair of
     // their taps, so a load takes a second wavefront when two such taps are
     // both hit and have tile offsets of equal parity
@@ -88,7 +89,7 @@ inline void bank_order(std::vector<int> &code, int Px, int PxPy, double J, int r
     };
     auto block_cost = [&](int blk) {
         long t = 0;
-        const int b = 32 * blk, e = b + 32 < n ? b + 32 : n;
+        const int b = kQ * blk, e = b + kQ < n ? b + kQ : n;
         for (int s = 0; s < S; ++s) {
             const uint8_t *sl = &slot[(size_t)s * n];
             int cnt[9] = {0}, mx = 0, q = 0;
@@ -119,7 +120,7 @@ inline void bank_order(std::vector<int> &code, int Px, int PxPy, double J, int r
         const int lo = 8 * c2, hi = lo + 8 < n ? lo + 8 : n;
         const int p2 = lo + (int)(uni() * (hi - lo));
         if ((p1 < ncore) != (p2 < ncore)) continue;
-        const int ca = p1 / 8, cb = p2 / 8, ba = p1 / 32, bb = p2 / 32;
+        const int ca = p1 / 8, cb = p2 / 8, ba = p1 / kQ, bb = p2 / kQ;
         std::swap(pos[p1], pos[p2]);
         const long na = chunk_cost(ca), nb = chunk_cost(cb);
         const long nba = block_cost(ba), nbb = ba != bb ? block_cost(bb) : 0;

@@ -593,7 +593,9 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             ig.n = (int)tab.size();
             const size_t plane = smem_plane_bytes(b->R, w);
             const size_t iplane = (size_t)(((plane / (w * sizeof(float2)) + 29) / 32) * 32 + 2) * w * 2 * sizeof(int);
-            ig.smem = std::max(plane, iplane) + cand_smem_bytes(maxcand) + 128;  // + tile alignment
+            // + tile alignment; the spread keeps its candidates as packed pairs
+            ig.smem = std::max(plane, iplane) +
+                      std::max(cand_smem_bytes(maxcand), cand_pairs_bytes(b->h_spr[0].cand)) + 128;
             int s2 = dalloc(b, &ig.tab, tab.size());
             if (s2 != NUFFT3D_SUCCESS) return bail(s2);
             if (cudaMemcpy(ig.tab, tab.data(), tab.size() * sizeof(int4), cudaMemcpyHostToDevice) != cudaSuccess)

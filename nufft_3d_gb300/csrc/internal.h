@@ -371,6 +371,8 @@ int run_inverse(nufft3d_plan *p, const float2 *raw, float2 *x, int nc, int maxit
 
 size_t smem_interp_bytes(const Geom &g, int cb);
 size_t cand_smem_bytes(int n);
+// shared memory of the spread's pair-interleaved candidate tables
+size_t cand_pairs_bytes(const Cand &cd);
 int interp_check_error();
 bool encode_gather_map(const nufft3d_plan *p, const float2 *G, int nc, int cb, CUtensorMap *m);  // reads and clears the interpolation timeout flag
 size_t smem_plane_bytes(int R, int cb);

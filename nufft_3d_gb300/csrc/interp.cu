@@ -91,6 +91,83 @@ __device__ __forceinline__ void build_cand(const Cand &cd, CandSmem cs)
 
 size_t cand_smem_bytes(int n) { return (size_t)(n + 6) * sizeof(float4); }
 
+// The spread's copy of the lists, for packed evaluation of two candidates per
+// lane: list q in blocks of 64, entry (b, l) holding its candidates 64b + l
+// ("a") and 64b + 32 + l ("b") as two words of bytes (dx'+8, dy'+8, dz'+8, 0),
+// one 8-byte shared load per lane and block (the spread is bound by
+// shared-memory traffic, not by issue).  Slots past the list's end hold byte
+// 255 per axis, an offset so far away that it never passes a support test.
+struct CandPairs {
+    const int *sc;  // [16]: first entry of list q, length of list q
+    const int2 *pc;
+};
+
+constexpr int kFarTapCode = 0x00FFFFFF;
+
+__host__ __device__ __forceinline__ int cand_pair_entries(const int *cnt)
+{
+    int n = 0;
+    for (int q = 0; q < 8; ++q) n += ((cnt[q] + 63) >> 6) * 32;
+    return n;
+}
+
+size_t cand_pairs_bytes(const Cand &cd)
+{
+    return (size_t)4 * sizeof(float4) + (((size_t)cand_pair_entries(cd.cnt) * sizeof(int2) + 15) & ~(size_t)15);
+}
+
+// Pair tables at the start of the dynamic shared memory; returns the first
+// free 16-byte word after them.
+__device__ __forceinline__ float4 *carve_pairs(const Cand &cd, CandPairs &cp, float4 *smem4)
+{
+    const int np = cand_pair_entries(cd.cnt);
+    cp.sc = reinterpret_cast<const int *>(smem4);
+    cp.pc = reinterpret_cast<const int2 *>(smem4 + 4);
+    return smem4 + 4 + (np + 1) / 2;
+}
+
+__device__ __forceinline__ void build_pairs(const Cand &cd, const CandPairs &cp)
+{
+    const int np = cand_pair_entries(cd.cnt);
+    if (threadIdx.x == 0) {
+        int *sc = const_cast<int *>(cp.sc);
+        int st = 0;
+        for (int q = 0; q < 8; ++q) {
+            sc[q] = st;
+            sc[8 + q] = cd.cnt[q];
+            st += ((cd.cnt[q] + 63) >> 6) * 32;
+        }
+    }
+    int2 *pc = const_cast<int2 *>(cp.pc);
+    for (int i = threadIdx.x; i < np; i += blockDim.x) {
+        int q = 0, st = 0;
+        for (; q < 7; ++q) {
+            const int n = ((cd.cnt[q] + 63) >> 6) * 32;
+            if (i < st + n) break;
+            st += n;
+        }
+        const int e = i - st, ia = 64 * (e >> 5) + (e & 31), ib = ia + 32;
+        int w[2];
+        const int idx[2] = {ia, ib};
+        for (int h = 0; h < 2; ++h) {
+            // the list's codes are 4 bits per axis with a bias of 8: widen to bytes
+            const int code = idx[h] < cd.cnt[q] ? cd.list[cd.start[q] + idx[h]] : -1;
+            w[h] = code < 0 ? kFarTapCode : (code & 15) | (((code >> 4) & 15) << 8) | (((code >> 8) & 15) << 16);
+        }
+        pc[i] = make_int2(w[0], w[1]);
+    }
+}
+
+// Axis k (byte k) of two pair codes as exact floats d' = byte - 8: the byte
+// is placed in the low mantissa bits of 1.5*2^23 and that bias removed.
+template <int K>
+__device__ __forceinline__ float2 pair_axis(const int2 c)
+{
+    const float2 m = make_float2(__int_as_float(__byte_perm(c.x, 0x4B400000, 0x7650 + K)),
+                                 __int_as_float(__byte_perm(c.y, 0x4B400000, 0x7650 + K)));
+    return __fadd2_rn(m, make_float2(-12582920.0f, -12582920.0f));
+}
+
 // Per-sample reflected coordinates.
 struct SampleGeo {
     float fx, fy, fz;  // |f|
@@ -118,6 +195,26 @@ __device__ __forceinline__ SampleGeo sample_geo(const float4 rec, int Px, int Py
     g.lbase = cs.sc[q];
     g.ln = cs.sc[8 + q];
     g.lcore = cs.sc[16 + q];
+    return g;
+}
+
+// The same for the pair tables: lbase = the list's first pair entry.
+__device__ __forceinline__ SampleGeo sample_geo_pairs(const float4 rec, int Px, int Py, const CandPairs &cp)
+{
+    SampleGeo g;
+    const int packed = __float_as_int(rec.w);
+    const int lx0 = packed & 0xFF, ly0 = (packed >> 8) & 0xFF, lz0 = (packed >> 16) & 0xFF;
+    g.sx = rec.x < 0.f ? -1.f : 1.f;
+    g.sy = rec.y < 0.f ? (float)-Px : (float)Px;
+    g.sz = rec.z < 0.f ? (float)(-Px * Py) : (float)(Px * Py);
+    g.fx = fabsf(rec.x);
+    g.fy = fabsf(rec.y);
+    g.fz = fabsf(rec.z);
+    g.b = (float)((lz0 * Py + ly0) * Px + lx0) + 12582912.0f;
+    const int q = (g.fx >= 0.25f ? 1 : 0) | (g.fy >= 0.25f ? 2 : 0) | (g.fz >= 0.25f ? 4 : 0);
+    g.lbase = cp.sc[q];
+    g.ln = cp.sc[8 + q];
+    g.lcore = 0;
     return g;
 }
 
@@ -167,30 +264,6 @@ __device__ __forceinline__ void tap_core(int ci, const SampleGeo &g, const CandS
     off = tap_offset(cf, g);
 }
 
-// Branch-free form of tap for the hot loops: the candidate index is clamped
-// into the list (so every load stays inside the tables and the tile) and the
-// weight is computed for every lane; the returned flag says whether the
-// candidate exists and lies inside the support.
-template <bool RADIAL>
-__device__ __forceinline__ bool tap_all(int ci, const SampleGeo &g, const CandSmem &cs, const KBParams &kb,
-                                        float &w, int &off)
-{
-    const bool valid = ci < g.ln;
-    const int cc = valid ? ci : g.ln - 1;
-    const float4 cf = cs.f[g.lbase + cc];
-    off = tap_offset(cf, g);
-    const float ex = cf.x - g.fx, ey = cf.y - g.fy, ez = cf.z - g.fz;
-    const float ex2 = ex * ex, ey2 = ey * ey, ez2 = ez * ez;
-    const float h2 = kb.half2;
-    if (RADIAL) {
-        const float d2 = ez2 + ey2 + ex2;
-        w = kb_weight(d2, kb);
-        return valid && d2 <= h2;
-    }
-    w = kb_weight(ez2, kb) * kb_weight(ey2, kb) * kb_weight(ex2, kb);
-    return valid && ex2 <= h2 && ey2 <= h2 && ez2 <= h2;
-}
-
 // Visit every (tile point, coil) of the padded tile with the grid point it
 // maps to: warps take tile rows (one division per row), lanes run along x and
 // the coil index (V values per point) so global accesses stay contiguous.
@@ -220,40 +293,76 @@ __device__ __forceinline__ void for_tile_rows(const Geom &g, int ox, int oy, int
     }
 }
 
-// Work layout of the spread: one warp per sample.  All 32 lanes evaluate 32
-// candidate taps at a time (weight + tile offset); the hits are compacted
-// through a per-warp queue and then applied by sub-steps in which lane (q, j)
-// handles queued tap j for coil pair q (NP pairs, CPS taps per sub-step).  A
-// quarter-warp adds 8 taps of one coil plane; the candidate order keeps their
-// offsets distinct modulo 8 where it can, so the reductions meet few bank
-// conflicts.  (The gather uses 8 lanes per sample instead, below.)
+// Work layout of the spread: one warp per sample.  The 32 lanes evaluate 64
+// candidate taps at a time, two per lane with packed FP32x2 arithmetic
+// (weight + tile offset); the hits are compacted through a per-warp queue
+// and then applied by sub-steps in which lane (q, j) handles queued tap j for
+// coil pair q (NP pairs, CPS taps per sub-step).  A quarter-warp adds 8 taps
+// of one coil plane; the candidate order keeps their offsets distinct modulo
+// 8 where it can, so the reductions meet few bank conflicts.  (The gather
+// uses 8 lanes per sample instead, below.)
 template <int CB>
 struct Lanes {
     static constexpr int NP = CB >= 2 ? CB / 2 : 1;  // coil pairs (or one coil)
     static constexpr int CPS = 32 / NP;               // queued taps per sub-step
 };
 
-struct TapQueue {
-    int2 e[32];  // (weight bits, tile offset): one 8-byte store and load per tap
+__device__ __forceinline__ float2 dup2(float v) { return make_float2(v, v); }
+
+// kb_weight for two distances at once: the polynomial with packed FP32x2
+// operations (the same rounding as the scalar steps), else two scalar calls.
+__device__ __forceinline__ float2 kb_weight2(float2 d2, const KBParams &p)
+{
+    if (p.poly) {
+        float2 t = __fmul2_rn(__fadd2_rn(dup2(p.half2), make_float2(-d2.x, -d2.y)), dup2(p.inv_half2));
+        t.x = fmaxf(t.x, 0.f);
+        t.y = fmaxf(t.y, 0.f);
+        float2 s = dup2(p.c[kKBDeg]);
+#pragma unroll
+        for (int k = kKBDeg - 1; k >= 0; --k) s = __ffma2_rn(s, t, dup2(p.c[k]));
+        return s;
+    }
+    return make_float2(kb_weight(d2.x, p), kb_weight(d2.y, p));
+}
+
+struct TapQueue2 {
+    int2 e[64];  // (weight bits, tile offset) of the hits of 64 candidates
 };
 
-// Evaluate candidates [base, base+32) of sample sg; returns the number of hits
-// written to the warp's queue (in lane order).
+// Evaluate candidates [base, base+64) of sample sg, two per lane with packed
+// FP32x2 arithmetic (lane l: candidates base+l and base+32+l); the hits go to
+// the warp's queue in list order.  Returns the hit count.
 template <bool RADIAL>
-__device__ __forceinline__ int eval_chunk(int base, const SampleGeo &sg, const CandSmem &cs,
-                                          const KBParams &kb, TapQueue &qu, int lane)
+__device__ __forceinline__ int eval_pair(int base, const SampleGeo &sg, const CandPairs &cp,
+                                         const KBParams &kb, TapQueue2 &qu, int lane)
 {
-    const int ci = base + lane;
-    float w = 0.f;
-    int off = 0;
-    const bool hit = tap_all<RADIAL>(ci, sg, cs, kb, w, off);
-    const unsigned m = __ballot_sync(0xffffffffu, hit);
-    if (hit) {
-        const int r = __popc(m & ((1u << lane) - 1u));
-        qu.e[r] = make_int2(__float_as_int(w), off);
+    const int2 cc = cp.pc[sg.lbase + (base >> 1) + lane];
+    const float2 X = pair_axis<0>(cc), Y = pair_axis<1>(cc), Z = pair_axis<2>(cc);
+    // tile offsets: base + s*d' summed on top of 1.5*2^23 (exact integers)
+    const float2 o = __ffma2_rn(Z, dup2(sg.sz), __ffma2_rn(Y, dup2(sg.sy), __ffma2_rn(X, dup2(sg.sx), dup2(sg.b))));
+    const float h2 = kb.half2;
+    float2 w;
+    bool ha, hb;
+    const float2 ex = __fadd2_rn(X, dup2(-sg.fx)), ey = __fadd2_rn(Y, dup2(-sg.fy)),
+                 ez = __fadd2_rn(Z, dup2(-sg.fz));
+    if (RADIAL) {
+        const float2 d2 = __ffma2_rn(ez, ez, __ffma2_rn(ey, ey, __fmul2_rn(ex, ex)));
+        ha = d2.x <= h2;
+        hb = d2.y <= h2;
+        w = kb_weight2(d2, kb);
+    } else {
+        const float2 ex2 = __fmul2_rn(ex, ex), ey2 = __fmul2_rn(ey, ey), ez2 = __fmul2_rn(ez, ez);
+        ha = ex2.x <= h2 && ey2.x <= h2 && ez2.x <= h2;
+        hb = ex2.y <= h2 && ey2.y <= h2 && ez2.y <= h2;
+        w = __fmul2_rn(__fmul2_rn(kb_weight2(ez2, kb), kb_weight2(ey2, kb)), kb_weight2(ex2, kb));
     }
+    const unsigned ma = __ballot_sync(0xffffffffu, ha), mb = __ballot_sync(0xffffffffu, hb);
+    const unsigned lt = (1u << lane) - 1u;
+    const int na = __popc(ma);
+    if (ha) qu.e[__popc(ma & lt)] = make_int2(__float_as_int(w.x), __float_as_int(o.x) - 0x4B400000);
+    if (hb) qu.e[na + __popc(mb & lt)] = make_int2(__float_as_int(w.y), __float_as_int(o.y) - 0x4B400000);
     __syncwarp();
-    return __popc(m);
+    return na + __popc(mb);
 }
 
 // Gather: tile staged coil-major ([CB][P^3] complex) -> ks.  kGroup lanes per
@@ -663,8 +772,8 @@ __device__ __forceinline__ void flush_tile(float2 *__restrict__ G, int nc, int c
 template <int CB, bool RADIAL, int R>
 __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
                                              const float4 *__restrict__ samples, const int4 bi, const Geom &g,
-                                             const KBParams &kb, const CandSmem &cs, int *tile, float *red,
-                                             TapQueue *queues)
+                                             const KBParams &kb, const CandPairs &cs, int *tile, float *red,
+                                             TapQueue2 *queues)
 {
     constexpr int NP = Lanes<CB>::NP, CPS = Lanes<CB>::CPS;
     constexpr int ps = IPlane<R>::PS;
@@ -678,7 +787,7 @@ __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, floa
     const int c = CB >= 2 ? 2 * q : 0;
     int *pl0 = tile + (size_t)(2 * c) * ps;  // re, im of coil c; then re, im of coil c+1
     const unsigned pl0_sa = (unsigned)__cvta_generic_to_shared(pl0);
-    TapQueue &qu = queues[warp];
+    TapQueue2 &qu = queues[warp];
     auto load_y = [&](int s, float4 &y) {
         const float2 *src = ks + (size_t)s * nc + c0;
         const float2 a = c < cb ? src[c] : make_float2(0.f, 0.f);
@@ -691,16 +800,14 @@ __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, floa
         load_y(bi.y + warp, y_next);
     }
     for (int s = bi.y + warp; s < send; s += nwarps) {
-        const SampleGeo sg = sample_geo(rec_next, Px, g.P[1], cs);
+        const SampleGeo sg = sample_geo_pairs(rec_next, Px, g.P[1], cs);
         const float4 y = y_next;
         if (s + nwarps < send) {
             rec_next = __ldg(&samples[s + nwarps]);
             load_y(s + nwarps, y_next);
         }
-        for (int base = 0; base < sg.ln; base += 32) {
-            // (a core-candidate path without the ballot, as in the gather,
-            // measured slower here)
-            const int nh = eval_chunk<RADIAL>(base, sg, cs, kb, qu, lane);
+        for (int base = 0; base < sg.ln; base += 64) {
+            const int nh = eval_pair<RADIAL>(base, sg, cs, kb, qu, lane);
             for (int t = j; t < nh; t += CPS) {
                 const int2 qe = qu.e[t];
                 const float w = __int_as_float(qe.x);
@@ -724,14 +831,14 @@ __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, floa
 }
 
 template <int R>
-__device__ __forceinline__ int *spread_setup(const Cand &cd, CandSmem &cs, float4 *smem4, int cbk)
+__device__ __forceinline__ int *spread_setup(const Cand &cd, CandPairs &cs, float4 *smem4, int cbk)
 {
     constexpr int ps = IPlane<R>::PS;
-    int *tile = reinterpret_cast<int *>(carve_cand(cd, cs, smem4));
+    int *tile = reinterpret_cast<int *>(carve_pairs(cd, cs, smem4));
     // zero the integer planes once, with 16-byte stores (ps * cbk * 2 is a multiple of 4)
     int4 *t4 = reinterpret_cast<int4 *>(tile);
     for (int t = threadIdx.x; t < ps * cbk / 2; t += blockDim.x) t4[t] = make_int4(0, 0, 0, 0);
-    build_cand(cd, cs);
+    build_pairs(cd, cs);
     __syncthreads();
     return tile;
 }
@@ -745,9 +852,9 @@ k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
 {
     extern __shared__ float4 smem4[];
     __shared__ float red[33];
-    __shared__ TapQueue queues[kInterpThreads / 32];
+    __shared__ TapQueue2 queues[kInterpThreads / 32];
     __shared__ int next;
-    CandSmem cs;
+    CandPairs cs;
     int *tile = spread_setup<R>(cd, cs, smem4, CB);
     for (;;) {
         if (threadIdx.x == 0) next = atomicAdd(work, 1);
@@ -1180,9 +1287,9 @@ k_spread_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ ta
 {
     extern __shared__ float4 smem4[];
     __shared__ float red[33];
-    __shared__ TapQueue queues[kInterpThreads / 32];
+    __shared__ TapQueue2 queues[kInterpThreads / 32];
     __shared__ int next;
-    CandSmem cs;
+    CandPairs cs;
     int *tile = spread_setup<R>(vols[0].cand, cs, smem4, CB);
     for (;;) {
         if (threadIdx.x == 0) next = atomicAdd(work, 1);
@@ -1326,7 +1433,7 @@ static int gather_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, int c0
 template <int CB, bool RADIAL, int R>
 static int spread_t(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, int c0, cudaStream_t s)
 {
-    const size_t smem = (size_t)IPlane<R>::PS * CB * 2 * sizeof(int) + cand_smem_bytes(p->n_cand);
+    const size_t smem = (size_t)IPlane<R>::PS * CB * 2 * sizeof(int) + cand_pairs_bytes(p->cand_desc);
     NUFFT_CUDA_TRY(cudaMemsetAsync(p->work + 1, 0, sizeof(int), s));
     const int64_t grid = std::min<int64_t>(p->n_blocks, p->sm_count);
     k_spread<CB, RADIAL, R><<<(unsigned)grid, kInterpThreads, smem, s>>>(

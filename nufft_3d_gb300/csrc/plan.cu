@@ -857,8 +857,10 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
     int cb = 1;
     while (cb * 2 <= cpp && cb < 8) cb *= 2;
     // the kernels also hold the candidate tables
-    const size_t cand_max =
-        cand_smem_bytes((int)candidate_set(R, g.radial, is2d, o.J, g.P[0], g.P[0] * g.P[1]).codes.size());
+    const CandSet &cset = candidate_set(R, g.radial, is2d, o.J, g.P[0], g.P[0] * g.P[1]);
+    Cand cnts{};
+    for (int q = 0; q < 8; ++q) cnts.cnt[q] = cset.cnt[q];
+    const size_t cand_max = std::max(cand_smem_bytes((int)cset.codes.size()), cand_pairs_bytes(cnts));
     while (cb > 1 && smem_plane_bytes(R, cb) + cand_max > 210 * 1024) cb /= 2;
     if (smem_plane_bytes(R, cb) + cand_max > 220 * 1024) {
         delete p;
