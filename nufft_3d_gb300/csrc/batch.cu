@@ -43,6 +43,7 @@ using namespace nufft3d;
 struct nufft3d_batch {
     int device = 0, nvol = 0, R = 0, radial = 1, is2d = 0, cb = 8;
     bool rare = false;
+    bool stored_h = false;  // every volume's plan holds its stored H
     std::vector<nufft3d_plan *> plans;
     std::vector<int> nc;
     // descriptor arrays (device) and their host mirrors
@@ -421,7 +422,7 @@ static int run_interp(nufft3d_batch *b, bool gather, cudaStream_t s)
 {
     for (auto &g : b->igroups)
         NUFFT_TRY(launch_interp_batch(gather, g.cb, b->R, b->radial, gather ? b->gat : b->spr, g.tab, g.n, g.smem,
-                                      b->plans[0]->kb, b->work, b->plans[0]->sm_count, s));
+                                      b->plans[0]->kb, b->work, b->plans[0]->sm_count, s, b->stored_h));
     return NUFFT3D_SUCCESS;
 }
 
@@ -577,6 +578,10 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             d.g = p->geom;
             d.kb = p->kb;
             d.cand = p->cand_desc;
+            d.tap_rows = p->tap_rows;
+            d.tap_ent = p->tap_ent;
+            if (v == 0) b->stored_h = true;
+            if (!p->tap_ent) b->stored_h = false;
             d.nc = nc[v];
             b->h_gat[v] = d;
             b->h_spr[v] = d;

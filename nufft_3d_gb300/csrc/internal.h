@@ -180,6 +180,8 @@ struct BatchInterp {
     int tmap_ok;               // bit log2(width): that map is valid
     int nc;
     float scale;
+    const uint32_t *tap_rows;  // the volume's stored H (8-coil gather entries), or null
+    const int2 *tap_ent;
 };
 
 struct BatchPerm {
@@ -212,8 +214,10 @@ struct BatchFFTParams {
 
 int batch_four_step(int K, bool all_vec16);
 int launch_fft_batch_p(const BatchFFTParams &P, int kind, size_t smem, bool rare, int r1, cudaStream_t s);
+// stored_h: every volume has its stored H (the 8-coil gather group then reads it)
 int launch_interp_batch(bool gather, int cb, int R, bool radial, const BatchInterp *vols, const int4 *table,
-                        int nblocks, size_t smem, const KBParams &kb, int *work, int nsm, cudaStream_t s);
+                        int nblocks, size_t smem, const KBParams &kb, int *work, int nsm, cudaStream_t s,
+                        bool stored_h);
 int launch_perm_batch(bool out, const BatchPerm *vols, const int4 *table, int nblocks, cudaStream_t s);
 
 // ----------------------------------------------------------------- plan

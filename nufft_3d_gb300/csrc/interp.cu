@@ -1280,6 +1280,36 @@ k_gather_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ ta
     }
 }
 
+// Batched 8-coil gather when every volume has its stored H: the table entry
+// (volume, piece, first coil) selects the volume's rows; shared memory = the
+// tile only.
+template <int R>
+__global__ void __launch_bounds__(kInterpThreads)
+k_gather_batch_tab(const BatchInterp *__restrict__ vols, const int4 *__restrict__ table, int ntab,
+                   int *__restrict__ work)
+{
+    extern __shared__ float4 smem4[];
+    __shared__ unsigned long long bar;
+    __shared__ int next;
+    float2 *tile = align128(smem4);
+    const unsigned bar_sa = (unsigned)__cvta_generic_to_shared(&bar);
+    if (threadIdx.x == 0) mbar_init(bar_sa, 1);
+    __syncthreads();
+    unsigned phase = 0;
+    for (;;) {
+        if (threadIdx.x == 0) next = atomicAdd(work, 1);
+        __syncthreads();
+        const int t = next;
+        if (t >= ntab) break;
+        const int4 e = table[t];
+        const BatchInterp &b = vols[e.x];
+        const CUtensorMap *tm = (b.tmap_ok >> 3) & 1 ? &b.tmaps[3] : nullptr;
+        if (!gather_piece_tab<R>(b.in, b.out, b.nc, e.z, b.blocks[e.y], b.g, b.scale, b.wsample, b.tap_rows,
+                                 b.tap_ent, tile, tm, bar_sa, phase))
+            return;
+    }
+}
+
 template <int CB, bool RADIAL, int R>
 __global__ void __launch_bounds__(kInterpThreads)
 k_spread_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ table, int ntab,
@@ -1636,9 +1666,22 @@ static int interp_batch_r(bool gather, int R, const BatchInterp *vols, const int
 }
 
 int launch_interp_batch(bool gather, int cb, int R, bool radial, const BatchInterp *vols, const int4 *table,
-                        int nblocks, size_t smem, const KBParams &kb, int *work, int nsm, cudaStream_t s)
+                        int nblocks, size_t smem, const KBParams &kb, int *work, int nsm, cudaStream_t s,
+                        bool stored_h)
 {
     if (nblocks <= 0) return NUFFT3D_SUCCESS;
+    if (gather && cb >= 8 && stored_h && R <= 3) {
+        NUFFT_CUDA_TRY(cudaMemsetAsync(work, 0, sizeof(int), s));
+        const int grid = nblocks < nsm ? nblocks : nsm;
+        const size_t sm = smem_plane_bytes(R, 8) + 128;
+        switch (R) {
+        case 1: k_gather_batch_tab<1><<<grid, kInterpThreads, sm, s>>>(vols, table, nblocks, work); break;
+        case 2: k_gather_batch_tab<2><<<grid, kInterpThreads, sm, s>>>(vols, table, nblocks, work); break;
+        default: k_gather_batch_tab<3><<<grid, kInterpThreads, sm, s>>>(vols, table, nblocks, work); break;
+        }
+        NUFFT_CUDA_TRY(cudaGetLastError());
+        return NUFFT3D_SUCCESS;
+    }
     if (cb >= 8) return radial ? interp_batch_r<8, true>(gather, R, vols, table, nblocks, smem, kb, work, nsm, s)
                                : interp_batch_r<8, false>(gather, R, vols, table, nblocks, smem, kb, work, nsm, s);
     if (cb >= 4) return radial ? interp_batch_r<4, true>(gather, R, vols, table, nblocks, smem, kb, work, nsm, s)
@@ -1704,6 +1747,9 @@ int configure_interp_kernels()
     NUFFT_TRY(allow_smem(k_tap_count<false>));
     NUFFT_TRY(allow_smem(k_tap_fill<true>));
     NUFFT_TRY(allow_smem(k_tap_fill<false>));
+    NUFFT_TRY(allow_smem(k_gather_batch_tab<1>));
+    NUFFT_TRY(allow_smem(k_gather_batch_tab<2>));
+    NUFFT_TRY(allow_smem(k_gather_batch_tab<3>));
     NUFFT_TRY(allow_smem(k_gather_tab<1>));
     NUFFT_TRY(allow_smem(k_gather_tab<2>));
     NUFFT_TRY(allow_smem(k_gather_tab<3>));
