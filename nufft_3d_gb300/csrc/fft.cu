@@ -331,6 +331,139 @@ k_line4(const float2 *__restrict__ in, float2 *__restrict__ out, LinePass lp, co
     line4_body<R1>(in, out, lp, twg, inv, blockIdx.x, sm);
 }
 
+// x passes as register four-step FFTs (K = 16*R1).  A block takes 16 lines,
+// a line being one (row yz, coil c) pair with the coil fastest, so any coil
+// count fills the blocks.  Forward (fNUFT.m:5 + nufft_3d.m:287-289, j=1):
+// image rows are contiguous, so the first phase reads with the point index
+// fastest (pad, shift and *U on the way in), and the coil-interleaved B1 is
+// written with the line index fastest.  Inverse (nufft_3d.m:296-298, j=1 +
+// aNUFT.m:8-9): B1 is read with the line index fastest and the rows go out
+// through shared memory in a third phase, contiguous, with the crop, *U*scale
+// and the optional addend; conj(FFT(conj x)) as in the other passes.
+template <int R1, bool INV>
+__global__ void __launch_bounds__(384)
+k_xline4(const float2 *__restrict__ in, float2 *__restrict__ out, const float *__restrict__ U,
+         const float2 *__restrict__ twg, int N1, int64_t N23, int nc, int64_t nlines, float scale,
+         const float2 *__restrict__ addend, float add_coef)
+{
+    constexpr int R2 = 16, K = R1 * R2, L = 16, LS = K + 1;
+    extern __shared__ float2 sm[];
+    float2 *Y = sm;
+    float2 *tw = sm + L * LS;
+    __shared__ int64_t rowb[L], intl[L];  // per line: image row start (c*N23 + yz)*N1, interleaved start yz*K*nc + c
+    __shared__ int64_t ub[L];             // U row start yz*N1, or -1 past the last line
+    for (int t = threadIdx.x; t < K; t += blockDim.x) tw[t] = twg[t];
+    if (threadIdx.x < L) {
+        const int64_t g = (int64_t)blockIdx.x * L + threadIdx.x;
+        if (g < nlines) {
+            const int64_t yz = g / nc;
+            const int c = (int)(g - yz * nc);
+            rowb[threadIdx.x] = ((int64_t)c * N23 + yz) * N1;
+            intl[threadIdx.x] = yz * K * nc + c;
+            ub[threadIdx.x] = yz * N1;
+        } else {
+            rowb[threadIdx.x] = intl[threadIdx.x] = 0;
+            ub[threadIdx.x] = -1;
+        }
+    }
+    const int Nh = N1 / 2, Nt = N1 - Nh;
+    __syncthreads();
+    // phase 1: DFT_R1 of the points n2 + 16*n1 of each column n2
+    for (int it = threadIdx.x; it < L * R2; it += blockDim.x) {
+        const int line = INV ? it % L : it / R2, n2 = INV ? it / L : it % R2;
+        const bool live = ub[line] >= 0;
+        float2 u[R1];
+#pragma unroll
+        for (int n1 = 0; n1 < R1; ++n1) {
+            const int pos = n2 + R2 * n1;
+            float2 v = make_float2(0.f, 0.f);
+            if (live) {
+                if (INV) {
+                    v = in[intl[line] + (int64_t)pos * nc];
+                    v.y = -v.y;
+                } else {
+                    // slot map (n - N1/2) mod K: slots [0, Nt) hold n = slot + N1/2,
+                    // slots [K - N1/2, K) hold n = slot - (K - N1/2), the rest zero padding
+                    const int src = pos < Nt ? pos + Nh : (pos >= K - Nh ? pos - (K - Nh) : -1);
+                    if (src >= 0) {
+                        const float2 x = in[rowb[line] + src];
+                        const float w = __ldg(&U[ub[line] + src]);
+                        v = make_float2(x.x * w, x.y * w);
+                    }
+                }
+            }
+            u[n1] = v;
+        }
+        dft_reg<R1>(u);
+#pragma unroll
+        for (int k1 = 0; k1 < R1; ++k1) {
+            float2 x = u[k1];
+            if (k1) x = cmul(x, tw[n2 * k1]);
+            Y[line * LS + k1 * R2 + n2] = x;
+        }
+    }
+    __syncthreads();
+    // phase 2: DFT_16 along each row of the exchange (one item per thread:
+    // blockDim >= 16*R1)
+    const bool act = threadIdx.x < L * R1;
+    const int line = threadIdx.x % L, k1 = threadIdx.x / L;
+    float2 u[R2];
+    if (act) {
+#pragma unroll
+        for (int n2 = 0; n2 < R2; ++n2) u[n2] = Y[line * LS + k1 * R2 + n2];
+        dft_reg<R2>(u);
+    }
+    if (!INV) {
+        if (act && ub[line] >= 0) {
+            float2 *ob = out + intl[line];
+#pragma unroll
+            for (int k2 = 0; k2 < R2; ++k2) ob[(int64_t)(k1 + R1 * k2) * nc] = u[k2];
+        }
+        return;
+    }
+    __syncthreads();  // every row has been read
+    if (act) {
+#pragma unroll
+        for (int k2 = 0; k2 < R2; ++k2) Y[line * LS + k1 + R1 * k2] = u[k2];
+    }
+    __syncthreads();
+    // phase 3: contiguous rows out
+    for (int it = threadIdx.x; it < L * N1; it += blockDim.x) {
+        const int ln = it / N1, n = it - ln * N1;
+        if (ub[ln] < 0) continue;
+        const float2 r = Y[ln * LS + slot_of(n, N1, K)];
+        const float w = __ldg(&U[ub[ln] + n]) * scale;
+        const int64_t idx = rowb[ln] + n;
+        float2 o = make_float2(r.x * w, -r.y * w);
+        if (addend) {
+            const float2 a = addend[idx];
+            o.x = fmaf(add_coef, a.x, o.x);
+            o.y = fmaf(add_coef, a.y, o.y);
+        }
+        out[idx] = o;
+    }
+}
+
+template <bool INV>
+static int launch_xline4(int r1, const float2 *in, float2 *out, const float *U, const FFTDesc &fd, int N1,
+                         int64_t N23, int nc, float scale, const float2 *addend, float add_coef, cudaStream_t s)
+{
+    const int K = fd.n;
+    const int threads = 16 * (r1 > 16 ? r1 : 16);
+    const size_t smem = (size_t)(16 * (K + 1) + K) * sizeof(float2);
+    const int64_t nlines = N23 * nc;
+    const unsigned nblk = (unsigned)((nlines + 15) / 16);
+    switch (r1) {
+    case 8: k_xline4<8, INV><<<nblk, threads, smem, s>>>(in, out, U, fd.tw, N1, N23, nc, nlines, scale, addend, add_coef); break;
+    case 12: k_xline4<12, INV><<<nblk, threads, smem, s>>>(in, out, U, fd.tw, N1, N23, nc, nlines, scale, addend, add_coef); break;
+    case 16: k_xline4<16, INV><<<nblk, threads, smem, s>>>(in, out, U, fd.tw, N1, N23, nc, nlines, scale, addend, add_coef); break;
+    case 20: k_xline4<20, INV><<<nblk, threads, smem, s>>>(in, out, U, fd.tw, N1, N23, nc, nlines, scale, addend, add_coef); break;
+    default: k_xline4<24, INV><<<nblk, threads, smem, s>>>(in, out, U, fd.tw, N1, N23, nc, nlines, scale, addend, add_coef); break;
+    }
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
 static int four_step_r1(int K, int vec)
 {
     if (vec != 16) return 0;
@@ -652,6 +785,8 @@ int launch_fx(nufft3d_plan *p, const float2 *img, float2 *B1, int nc, cudaStream
 {
     const int N1 = p->N[0], N23 = p->N[1] * p->N[2];
     const FFTDesc &fd = p->fft[0];
+    if (const int r1 = four_step_r1(fd.n, 16))
+        return launch_xline4<false>(r1, img, B1, p->U, fd, N1, N23, nc, 1.f, nullptr, 0.f, s);
     const int nv = nc < kMaxLineCoils ? nc : kMaxLineCoils;
     dim3 grid(N23, (nc + kMaxLineCoils - 1) / kMaxLineCoils);
     if (needs_rare(fd))
@@ -667,6 +802,8 @@ int launch_ix(nufft3d_plan *p, const float2 *B1, float2 *img, int nc, float scal
 {
     const int N1 = p->N[0], N23 = p->N[1] * p->N[2];
     const FFTDesc &fd = p->fft[0];
+    if (const int r1 = four_step_r1(fd.n, 16))
+        return launch_xline4<true>(r1, B1, img, p->U, fd, N1, N23, nc, scale, addend, add_coef, s);
     const int nv = nc < kMaxLineCoils ? nc : kMaxLineCoils;
     dim3 grid(N23, (nc + kMaxLineCoils - 1) / kMaxLineCoils);
     if (needs_rare(fd))
@@ -735,6 +872,16 @@ int configure_fft_kernels()
     NUFFT_TRY(allow_fft_smem(k_fx<true>));
     NUFFT_TRY(allow_fft_smem(k_ix<true>));
     NUFFT_TRY(allow_fft_smem(k_line<true>));
+    NUFFT_TRY(allow_fft_smem(k_xline4<8, false>));
+    NUFFT_TRY(allow_fft_smem(k_xline4<12, false>));
+    NUFFT_TRY(allow_fft_smem(k_xline4<16, false>));
+    NUFFT_TRY(allow_fft_smem(k_xline4<20, false>));
+    NUFFT_TRY(allow_fft_smem(k_xline4<24, false>));
+    NUFFT_TRY(allow_fft_smem(k_xline4<8, true>));
+    NUFFT_TRY(allow_fft_smem(k_xline4<12, true>));
+    NUFFT_TRY(allow_fft_smem(k_xline4<16, true>));
+    NUFFT_TRY(allow_fft_smem(k_xline4<20, true>));
+    NUFFT_TRY(allow_fft_smem(k_xline4<24, true>));
     NUFFT_TRY(allow_fft_smem(k_line4<8>));
     NUFFT_TRY(allow_fft_smem(k_line4<12>));
     NUFFT_TRY(allow_fft_smem(k_line4<16>));
