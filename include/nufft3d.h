@@ -62,7 +62,7 @@ typedef struct nufft3d_opts {
     int density_iters; /* density.m:5 maxit (default 20) */
     int tile[3];       /* interpolation tile shape (0 = autotune/default) */
     int max_coils_per_pass; /* coils handled per interpolation pass (0 = auto) */
-    int max_samples_per_block; /* samples per interpolation block (0 = auto) */
+    int max_samples_per_block; /* samples per interpolation block (0 = 4096) */
     int verbose;       /* print the reference's set-up summary to stdout */
     int tap_table;     /* stored interpolation matrix H (nufft_3d.m:153-212) in
                           tile order, read by the 8-coil gather passes of fNUFT

@@ -626,7 +626,7 @@ static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts
     p->nnz = nnz;
 
     // tile pieces of at most S samples, split evenly
-    const int S = o.max_samples_per_block > 0 ? o.max_samples_per_block : 2048;
+    const int S = o.max_samples_per_block > 0 ? o.max_samples_per_block : 4096;  // larger pieces measured slightly faster (fewer halo flushes)
     std::vector<int4> blocks;
     int64_t off = 0;
     for (uint32_t t = 0; t < ntiles; ++t) {
