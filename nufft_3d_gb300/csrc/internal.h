@@ -297,7 +297,8 @@ struct nufft3d_plan {
     int coils_per_pass = 8;
     int use_tma = 1;            // bulk tensor copies for interior gather tiles
     int sm_count = 148;         // multiprocessors of the plan's device
-    int *work = nullptr;        // work counter of the persistent interpolation kernels
+    int *work = nullptr;        // [16]: work counters of the persistent interpolation kernels (0 gather,
+                                // 1 spread), 2 the stored-H build's error flag
     // stored H in tile order (8-coil passes): row of sorted sample s = entries
     // [8*tap_rows[s], 8*tap_rows[s+1]) of tap_ent, (weight bits, tile offset),
     // padded with zero weights to whole chunks of 8

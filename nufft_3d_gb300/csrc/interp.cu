@@ -1084,8 +1084,6 @@ __device__ __forceinline__ bool tap_exact(int ci, const SampleGeo &g, const Cand
     return true;
 }
 
-__device__ unsigned g_tap_err;  // set when a fill pass finds more hits than its row holds
-
 // Plan time, pass 1 of the stored H: rows[s] = 8-entry chunks of sample s's
 // row (its hits, rounded up).  One warp per sample.
 template <bool RADIAL>
@@ -1116,11 +1114,12 @@ k_tap_count(const float4 *__restrict__ samples, int64_t nnz, Geom g, KBParams kb
 
 // Plan time, pass 2: the entries of every row in bank order (see above).
 // Per warp two shared buffers of cap entries: the hits in candidate order,
-// then in round-robin residue order.
+// then in round-robin residue order.  *err is set if a row has more hits
+// than the count pass found (the row is then cut at its length).
 template <bool RADIAL>
 __global__ void __launch_bounds__(256)
 k_tap_fill(const float4 *__restrict__ samples, int64_t nnz, Geom g, KBParams kb, const __grid_constant__ Cand cd,
-           const uint32_t *__restrict__ rows, int2 *__restrict__ taps, int cap)
+           const uint32_t *__restrict__ rows, int2 *__restrict__ taps, int cap, int *__restrict__ err)
 {
     extern __shared__ float4 smem4[];
     CandSmem cs;
@@ -1147,7 +1146,7 @@ k_tap_fill(const float4 *__restrict__ samples, int64_t nnz, Geom g, KBParams kb,
         const size_t row = (size_t)__ldg(&rows[s]) * 8;
         const int nfill = (int)((size_t)__ldg(&rows[s + 1]) * 8 - row);
         if (nh > nfill) {
-            if (lane == 0) atomicOr(&g_tap_err, 1u);
+            if (lane == 0) atomicOr(err, 1);
             nh = nfill;
         }
         // hits per residue of the tile offset mod 8
@@ -1586,22 +1585,22 @@ int launch_tap_count(nufft3d_plan *p, uint32_t *rows, cudaStream_t s)
 int launch_tap_fill(nufft3d_plan *p, const uint32_t *rows, int2 *taps, cudaStream_t s)
 {
     if (p->nnz == 0) return NUFFT3D_SUCCESS;
-    const unsigned zero = 0;
-    NUFFT_CUDA_TRY(cudaMemcpyToSymbolAsync(g_tap_err, &zero, sizeof(zero), 0, cudaMemcpyHostToDevice, s));
+    int *err = p->work + 2;  // the plan's own flag (plans may be built concurrently)
+    NUFFT_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
     int cap = 0;
     for (int q = 0; q < 8; ++q) cap = std::max(cap, p->cand_desc.cnt[q]);
     const size_t smem = cand_smem_bytes(p->n_cand) + (size_t)8 * 2 * cap * sizeof(int2);
     if (smem > 200 * 1024) return fail(NUFFT3D_ERR_UNSUPPORTED, "candidate lists too long for the stored H");
     const unsigned nb = (unsigned)std::min<int64_t>((p->nnz + 7) / 8, (int64_t)p->sm_count * 8);
     if (p->geom.radial)
-        k_tap_fill<true><<<nb, 256, smem, s>>>(p->samples, p->nnz, p->geom, p->kb, cand_of(p), rows, taps, cap);
+        k_tap_fill<true><<<nb, 256, smem, s>>>(p->samples, p->nnz, p->geom, p->kb, cand_of(p), rows, taps, cap, err);
     else
-        k_tap_fill<false><<<nb, 256, smem, s>>>(p->samples, p->nnz, p->geom, p->kb, cand_of(p), rows, taps, cap);
+        k_tap_fill<false><<<nb, 256, smem, s>>>(p->samples, p->nnz, p->geom, p->kb, cand_of(p), rows, taps, cap, err);
     NUFFT_CUDA_TRY(cudaGetLastError());
-    unsigned err = 0;
-    NUFFT_CUDA_TRY(cudaMemcpyFromSymbolAsync(&err, g_tap_err, sizeof(err), 0, cudaMemcpyDeviceToHost, s));
+    int herr = 0;
+    NUFFT_CUDA_TRY(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, s));
     NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
-    if (err) return fail(NUFFT3D_ERR_CUDA, "stored H: fill pass disagrees with the count pass");
+    if (herr) return fail(NUFFT3D_ERR_CUDA, "stored H: fill pass disagrees with the count pass");
     return NUFFT3D_SUCCESS;
 }
 
