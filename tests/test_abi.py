@@ -33,6 +33,25 @@ def test_opts_struct_layout_matches_defaults():
     o = _lib.Opts()
     assert L.nufft3d_opts_default(ctypes.byref(o)) == 0
     assert (o.J, o.u, o.alpha, o.radial, o.gpu, o.density_iters) == (4.0, 2.0, 0.0, 1, 1, 20)
+    assert o.tap_table == -1  # the stored H is built when it fits (last field: the layout matches the header)
+
+
+def test_header_struct_fields_match_ctypes():
+    """Every field of nufft3d_opts / nufft3d_info in include/nufft3d.h is mirrored, in order."""
+    import os, re
+    hdr = open(os.path.join(os.path.dirname(__file__), "..", "include", "nufft3d.h")).read()
+    for cname, cls in (("nufft3d_opts", _lib.Opts), ("nufft3d_info", _lib.Info)):
+        body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (cname, cname), hdr, re.S).group(1)
+        body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+        names = []
+        for decl in body.split(";"):
+            if not decl.strip():
+                continue
+            parts = decl.split(",")  # "double J, u, alpha"
+            for i, part in enumerate(parts):
+                word = part.split()[-1] if i == 0 else part.strip()
+                names.append(re.sub(r"\[.*\]", "", word.lstrip("*")))
+        assert names == [f[0] for f in cls._fields_], (cname, names)
 
 
 def _create(om, N, **kw):
