@@ -181,7 +181,7 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
         _lib.check(self._L.nufft3d_plan_info(self.plan, ctypes.byref(i)))
         return {"N": list(i.N), "K": list(i.K), "M": i.M, "nnz": i.nnz, "tile": list(i.tile),
                 "n_blocks": i.n_blocks, "taps_per_sample": i.taps_per_sample,
-                "device_bytes": i.device_bytes}
+                "device_bytes": i.device_bytes, "tap_table_bytes": i.tap_table_bytes}
 
     # --------------------------------------------------------- operators
     def _coils_img(self, x):

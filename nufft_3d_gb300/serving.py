@@ -129,7 +129,14 @@ class ReconServer:
         K = 2 * int(np.ceil(N * req.opts.get("u", 2) / 2))
         M = req.om.shape[1] if req.om.ndim == 2 else req.om.size // 3
         # sorted records, perm, inv, d, d_orig, U, tiles
-        return M * (16 + 4 + 4 + 4 + 4) + N ** 3 * 4 + (K // 8 + 1) ** 3 * 20
+        b = M * (16 + 4 + 4 + 4 + 4) + N ** 3 * 4 + (K // 8 + 1) ** 3 * 20
+        # the stored H (8-byte entries, rows padded to chunks of 8) that plans
+        # with ceil(J/2) <= 3 build when it fits
+        J = float(req.opts.get("J", 4))
+        if int(np.ceil(J / 2)) <= 3:
+            taps = 4.0 / 3.0 * np.pi * (J / 2) ** 3 if req.opts.get("radial", 1) else J ** 3
+            b += int(M * ((taps + 4) * 8 + 4))
+        return b
 
     @staticmethod
     def _work_bytes(req, nc):
@@ -155,12 +162,15 @@ class ReconServer:
                 coils += r.nc
         return batch, coils
 
-    def _evict_for(self, need):
+    def _evict_for(self, need, slot, keep):
+        # the requesting slot's own handle does not pin its key: the slot
+        # closes that handle before it runs the new batch (the tables go with
+        # the last handle); the key the request needs stays
         for key in list(self.cache):
             if self.used + need <= self.budget:
                 break
             e = self.cache[key]
-            if e["users"] == 0 and all(r[0] != key for r in self.slot_res):
+            if key != keep and e["users"] == 0 and all(r[0] != key for i, r in enumerate(self.slot_res) if i != slot):
                 e["plan"].close()
                 self.used -= e["bytes"]
                 del self.cache[key]
@@ -183,7 +193,7 @@ class ReconServer:
         pbytes = self._plan_bytes_estimate(req0) if new_plan else 0
         need = extra + pbytes
         if self.used + need > self.budget:
-            self._evict_for(need)
+            self._evict_for(need, slot, req0.key)
         if self.used + need > self.budget and any(e["users"] for e in self.cache.values()):
             return None           # wait for memory to be released by running work
         for item in batch:
