@@ -932,8 +932,10 @@ __device__ __forceinline__ int2 ld_tap(const int2 *p)
 // form one contiguous stream of chunks; lane l of the group applies entry l
 // of every chunk (a whole tap: 8 coils, rotated coil-pair reads as in the
 // on-the-fly gather) and keeps the next 4 chunks' entries in registers, so
-// the loads run ahead across sample boundaries (2, 3 or 6 chunks measured
-// slower).  At the end of a sample the group reduces its 8 partial sums.
+// the loads run ahead across sample boundaries (2, 3 or 6 chunks in
+// registers, a 5-deep per-lane shared-memory FIFO filled by asynchronous
+// copies, and L2 prefetch windows all measured slower).  At the end of a
+// sample the group reduces its 8 partial sums.
 template <int R>
 __device__ __forceinline__ bool gather_piece_tab(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc,
                                                  int c0, const int4 bi, const Geom &g, float scale,
