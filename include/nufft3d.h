@@ -69,6 +69,13 @@ typedef struct nufft3d_opts {
                           (H' is applied on the fly): 1 = build it, 0 = evaluate
                           the kernel on the fly, -1 = auto (default: build it
                           when it takes at most half of the free device memory) */
+    int wait_polls;    /* polls of each bounded wait of the interpolation
+                          kernels (the tile copy of the gather) before it gives
+                          up and reports NUFFT3D_ERR_TIMEOUT (default 2^22, well
+                          under a second); 0 gives up at once: every bulk tile
+                          copy is then still allowed to land, but its tile is
+                          skipped and the timeout reported, which exercises the
+                          error path without a fault */
 } nufft3d_opts;
 
 /* Read-only properties (nufft_3d.m:26-43). */
@@ -228,6 +235,19 @@ int nufft3d_profile(nufft3d_plan *plan, int enable);
  * {"gather": {"calls": C, "launches": L, "ms": T}, ...}.  Synchronises on the
  * recorded events. */
 int nufft3d_profile_read(nufft3d_plan *plan, char *buf, int cap);
+
+/* Status of the asynchronous work of a plan: reads and clears the plan's
+ * status flag after the work queued on `stream` (the stream the device-pointer
+ * calls ran on; NULL = the legacy default stream) and synchronises that
+ * stream.  Returns NUFFT3D_ERR_TIMEOUT if a bounded wait in an interpolation
+ * kernel expired since the last check (the affected tiles were skipped, so
+ * those results are incomplete), else NUFFT3D_SUCCESS.  Device-pointer calls
+ * (nufft3d_forward, _adjoint, _normal, _inverse*, nufft3d_forward_noalloc and
+ * the batch calls, which report on the plans of their volumes) return before
+ * their kernels run and report through this call; the host-pointer calls and
+ * nufft3d_density check it themselves.  No counterpart in the reference,
+ * whose MATLAB operators are synchronous. */
+int nufft3d_check_status(nufft3d_plan *plan, void *stream);
 
 /* Message of the last failed call on this thread ("" if none). */
 const char *nufft3d_last_error(void);

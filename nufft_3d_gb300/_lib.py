@@ -40,7 +40,7 @@ class Opts(ctypes.Structure):
                 ("d", ctypes.c_void_p), ("density_iters", ctypes.c_int),
                 ("tile", ctypes.c_int * 3), ("max_coils_per_pass", ctypes.c_int),
                 ("max_samples_per_block", ctypes.c_int), ("verbose", ctypes.c_int),
-                ("tap_table", ctypes.c_int)]
+                ("tap_table", ctypes.c_int), ("wait_polls", ctypes.c_int)]
 
 
 class Info(ctypes.Structure):
@@ -88,6 +88,7 @@ SIGNATURES = {
     "nufft3d_batch_forward": (ctypes.c_int, [_P, _P, _P, _P]),
     "nufft3d_batch_adjoint": (ctypes.c_int, [_P, _P, _P, _P]),
     "nufft3d_batch_inverse": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, _P, _P]),
+    "nufft3d_check_status": (ctypes.c_int, [_P, _P]),
     "nufft3d_profile": (ctypes.c_int, [_P, ctypes.c_int]),
     "nufft3d_profile_read": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int]),
     "nufft3d_last_error": (ctypes.c_char_p, []),

@@ -425,8 +425,7 @@ static int host_call(nufft3d_plan *p, const void *in, void *out, size_t bi, size
     }
     NUFFT_TRY(op((const float2 *)din, dout ? (float2 *)dout : (float2 *)p->stage.out, s));
     if (!dout) NUFFT_CUDA_TRY(cudaMemcpyAsync(out, p->stage.out, bo, cudaMemcpyDeviceToHost, s));
-    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
-    NUFFT_TRY(interp_check_error());
+    NUFFT_TRY(plan_check_status(p, s));
     return NUFFT3D_SUCCESS;
 }
 
@@ -459,9 +458,16 @@ extern "C" int nufft3d_density(nufft3d_plan *p, int maxit)
     if (maxit < 0) return fail(NUFFT3D_ERR_ARG, "maxit must be nonnegative");
     DevGuard g(p->device);
     NUFFT_TRY(run_density(p, maxit, p->own_stream));
-    NUFFT_CUDA_TRY(cudaStreamSynchronize(p->own_stream));
-    NUFFT_TRY(interp_check_error());
+    NUFFT_TRY(plan_check_status(p, p->own_stream));
     return NUFFT3D_SUCCESS;
+}
+
+extern "C" int nufft3d_check_status(nufft3d_plan *p, void *stream)
+{
+    clear_error();
+    if (!p) return fail(NUFFT3D_ERR_ARG, "plan is NULL");
+    DevGuard g(p->device);
+    return plan_check_status(p, (cudaStream_t)stream);
 }
 
 extern "C" int nufft3d_profile(nufft3d_plan *p, int enable)

@@ -580,6 +580,7 @@ extern "C" int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, i
             d.cand = p->cand_desc;
             d.tap_rows = p->tap_rows;
             d.tap_ent = p->tap_ent;
+            d.status = plan_status(p);  // timeouts are reported on the volume's plan
             if (v == 0) b->stored_h = true;
             if (!p->tap_ent) b->stored_h = false;
             d.nc = nc[v];

@@ -167,6 +167,20 @@ struct Cand {
     int core[8];    // its first core[q] entries are inside the support for every sample of the sub-cube
 };
 
+// Status of the interpolation kernels of one plan: where an expired bounded
+// wait is reported and how many polls a wait makes.
+struct InterpStatus {
+    int *err;   // the plan's status flag (set to 1 on expiry), or null
+    int polls;  // polls of each bounded wait
+};
+
+// Slots of a plan's small device work buffer (int[16]).
+constexpr int kWorkGather = 0;   // work counter of the persistent gather
+constexpr int kWorkSpread = 1;   // work counter of the persistent spread
+constexpr int kWorkTapFill = 2;  // stored-H build: fill disagrees with count
+constexpr int kWorkStatus = 3;   // interpolation status (a bounded wait expired)
+constexpr int kDefaultWaitPolls = 1 << 22;
+
 struct BatchInterp {
     const float2 *in;   // gather: grid; spread: sorted samples
     float2 *out;        // gather: sorted samples; spread: grid
@@ -182,6 +196,7 @@ struct BatchInterp {
     float scale;
     const uint32_t *tap_rows;  // the volume's stored H (8-coil gather entries), or null
     const int2 *tap_ent;
+    InterpStatus status;       // the volume's plan: its status flag and wait polls
 };
 
 struct BatchPerm {
@@ -297,8 +312,9 @@ struct nufft3d_plan {
     int coils_per_pass = 8;
     int use_tma = 1;            // bulk tensor copies for interior gather tiles
     int sm_count = 148;         // multiprocessors of the plan's device
-    int *work = nullptr;        // [16]: work counters of the persistent interpolation kernels (0 gather,
-                                // 1 spread), 2 the stored-H build's error flag
+    int *work = nullptr;        // [16]: work counters of the persistent interpolation kernels and the
+                                // plan's status flags (slots kWork*)
+    int wait_polls = nufft3d::kDefaultWaitPolls;  // polls of each bounded wait in the gather
     // stored H in tile order (8-coil passes): row of sorted sample s = entries
     // [8*tap_rows[s], 8*tap_rows[s+1]) of tap_ent, (weight bits, tile offset),
     // padded with zero weights to whole chunks of 8
@@ -378,8 +394,11 @@ size_t smem_interp_bytes(const Geom &g, int cb);
 size_t cand_smem_bytes(int n);
 // shared memory of the spread's pair-interleaved candidate tables
 size_t cand_pairs_bytes(const Cand &cd);
-int interp_check_error();
-bool encode_gather_map(const nufft3d_plan *p, const float2 *G, int nc, int cb, CUtensorMap *m);  // reads and clears the interpolation timeout flag
+// Reads and clears the plan's interpolation status flag on stream s (after
+// the work queued there): NUFFT3D_ERR_TIMEOUT if a bounded wait expired.
+int plan_check_status(nufft3d_plan *p, cudaStream_t s);
+InterpStatus plan_status(const nufft3d_plan *p);
+bool encode_gather_map(const nufft3d_plan *p, const float2 *G, int nc, int cb, CUtensorMap *m);
 size_t smem_plane_bytes(int R, int cb);
 
 // Stage timing scope: records an event pair on stream s when profiling is on

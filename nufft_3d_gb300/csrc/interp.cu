@@ -373,8 +373,10 @@ __device__ __forceinline__ int eval_pair(int base, const SampleGeo &sg, const Ca
 // grid [K3][K2][K1][nc] complex (4-D map: 2*nc floats, K1, K2, K3), which
 // lands point-major in shared memory.  Tiles that wrap around the grid edge
 // use per-element asynchronous copies into the same layout.
-// Waits are bounded: on expiry g_interp_err is set and the block returns.
-__device__ unsigned g_interp_err;
+// Waits are bounded (a plan option gives the number of polls): on expiry
+// the block sets its plan's status flag (read by nufft3d_check_status and
+// the host-pointer entry points), lets the copy land with a second bounded
+// wait and returns.
 
 __device__ __forceinline__ void mbar_init(unsigned bar, unsigned count)
 {
@@ -421,13 +423,17 @@ __device__ __forceinline__ bool tile_origin(const Geom &g, int tid, int &ox, int
            oz + g.P[2] <= g.K[2];
 }
 
-// Bounded wait for the phase of the given parity; false if it expired.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity)
+// Bounded wait for the phase of the given parity (at most `polls` polls);
+// false if it expired.
+constexpr int kDrainPolls = 1 << 22;
+
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned bar, unsigned parity, int polls)
 {
-    for (int i = 0; i < (1 << 22); ++i)
+    for (int i = 0; i < polls; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+
 
 __device__ __forceinline__ float2 *align128(float4 *p)
 {
@@ -494,7 +500,7 @@ __device__ __forceinline__ void unrotate(float2 (&acc)[CB], int rot)
 template <int CB>
 __device__ __forceinline__ bool stage_tile(const float2 *__restrict__ G, int nc, int c0, const int4 bi,
                                            const Geom &g, float2 *tile, const CUtensorMap *tmap, unsigned bar_sa,
-                                           unsigned &phase)
+                                           unsigned &phase, const InterpStatus &st)
 {
     int ox, oy, oz;
     const bool inside = tile_origin(g, bi.x, ox, oy, oz);
@@ -505,13 +511,14 @@ __device__ __forceinline__ bool stage_tile(const float2 *__restrict__ G, int nc,
             mbar_expect_tx(bar_sa, (unsigned)(g.P[0] * g.P[1] * g.P[2] * CB * sizeof(float2)));
             tma_load_4d((unsigned)__cvta_generic_to_shared(tile), tmap, 2 * c0, ox, oy, oz, bar_sa);
         }
-        const bool done = mbar_wait_bounded(bar_sa, phase);
+        const bool done = mbar_wait_bounded(bar_sa, phase, st.polls);
         phase ^= 1u;
         if (__syncthreads_or(!done)) {     // block-uniform exit on expiry
             if (threadIdx.x == 0) {
-                atomicOr(&g_interp_err, 1u);
-                mbar_wait_bounded(bar_sa, phase ^ 1u);  // let the copy land before the block exits
+                if (st.err) atomicOr(st.err, 1);
+                mbar_wait_bounded(bar_sa, phase ^ 1u, kDrainPolls);  // let the copy land before the block exits
             }
+            __syncthreads();
             return false;
         }
     } else {
@@ -542,9 +549,9 @@ __device__ __forceinline__ bool gather_piece(const float2 *__restrict__ G, float
                                              const float4 *__restrict__ samples, const int4 bi, const Geom &g,
                                              const KBParams &kb, float scale, const float *__restrict__ wsample,
                                              const CandSmem &cs, float2 *tile, const CUtensorMap *tmap,
-                                             unsigned bar_sa, unsigned &phase)
+                                             unsigned bar_sa, unsigned &phase, const InterpStatus &st)
 {
-    if (!stage_tile<CB>(G, nc, c0, bi, g, tile, tmap, bar_sa, phase)) return false;
+    if (!stage_tile<CB>(G, nc, c0, bi, g, tile, tmap, bar_sa, phase, st)) return false;
     const int Px = g.P[0];
     const int cb = min(CB, nc - c0);
     const int lane = threadIdx.x & 31;
@@ -632,7 +639,7 @@ __global__ void __launch_bounds__(kInterpThreads)
 k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
          const float4 *__restrict__ samples, const int4 *__restrict__ blocks, int nblocks, int *__restrict__ work,
          Geom g, KBParams kb, float scale, const float *__restrict__ wsample, const __grid_constant__ Cand cd,
-         const __grid_constant__ CUtensorMap tmap, int use_tma)
+         const __grid_constant__ CUtensorMap tmap, int use_tma, InterpStatus st)
 {
     extern __shared__ float4 smem4[];
     __shared__ unsigned long long bar;
@@ -645,18 +652,20 @@ k_gather(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
         const int b = next;
         if (b >= nblocks) break;
         if (!gather_piece<CB, RADIAL, R>(G, ks, nc, c0, samples, blocks[b], g, kb, scale, wsample, m.cs, m.tile,
-                                         use_tma ? &tmap : nullptr, m.bar_sa, phase))
+                                         use_tma ? &tmap : nullptr, m.bar_sa, phase, st))
             return;
     }
 }
 
 // Spread: ks -> tile -> grid.  The tile accumulates in 32-bit fixed point
 // with native shared-memory integer reductions (floating-point shared atomics
-// are several times slower on this part).  Per block and call the scale is a
-// power of two 2^F chosen from the largest |Re|,|Im| of the block's samples
-// and the plan-time bound wsum = max over tile points of the summed weights,
-// so that every partial sum stays below 2^30 and every product w*y*2^F below
-// 2^22; products are rounded to integers exactly by the 1.5*2^23 addition.
+// are several times slower on this part).  Per piece and coil the scale is a
+// power of two 2^F chosen from that coil's largest |Re|,|Im| over the piece's
+// samples and the plan-time bound wsum = max over tile points of the summed
+// weights, so that every partial sum stays below 2^30 and every product
+// w*y*2^F below 2^22; products are rounded to integers exactly by the
+// 1.5*2^23 addition.  Each coil keeps its own precision whatever the gain of
+// the other coils of the pass (coils of unrelated requests can share a pass).
 // Layout [CB][2][P^3] int32 (split real/imaginary planes, so a warp's
 // scattered taps spread over all banks).  A warp takes one sample: its hits
 // are compacted into a queue and each quarter-warp adds one coil pair of 8
@@ -703,38 +712,67 @@ struct IPlane {
     static constexpr int PS = ((Plane<R>::PS + 29) / 32) * 32 + 2;
 };
 
-// Fixed-point scale 2^F of a spread piece from its largest |Re|,|Im| and the
-// plan-time bound on summed weights; false (block-uniform) when the piece
-// adds nothing.  Contains __syncthreads.
+// Per-coil fixed-point scales of a spread piece: psc[c] = 2^F_c and
+// psc[kMaxCB + c] = 2^-F_c from coil c's largest |Re|,|Im| over the piece
+// and the plan-time bound on summed weights (coils that are zero over the
+// piece get F = 0: they add nothing).  red holds 32*CB floats.  Returns
+// false (block-uniform) when the piece adds nothing.  Contains __syncthreads.
+constexpr int kMaxCB = 8;
+
+template <int CB>
 __device__ __forceinline__ bool piece_scale(const float2 *__restrict__ ks, int nc, int c0, int cb, const int4 bi,
-                                            float *red, float &scale, float &inv_scale)
+                                            float *red, float *psc)
 {
     const int send = bi.y + bi.z;
-    float m = 0.f;
+    float m[CB];
+#pragma unroll
+    for (int c = 0; c < CB; ++c) m[c] = 0.f;
     for (int s = bi.y + threadIdx.x; s < send; s += blockDim.x) {
         const float2 *src = ks + (size_t)s * nc + c0;
-        for (int c = 0; c < cb; ++c) {
-            const float2 v = src[c];
-            m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
+#pragma unroll
+        for (int c = 0; c < CB; ++c) {
+            if (c < cb) {
+                const float2 v = src[c];
+                m[c] = fmaxf(m[c], fmaxf(fabsf(v.x), fabsf(v.y)));
+            }
         }
     }
-    const float ymax = block_max(m, red);
-    if (!(ymax > 0.f)) return false;
-    const float wsum = fmaxf(__int_as_float(bi.w), 1.0f);
-    int ey, ecy;
-    frexpf(ymax, &ey);                     // ymax < 2^ey
-    frexpf(ymax * wsum, &ecy);             // wsum*ymax < 2^ecy
-    const int F = min(22 - ey, 30 - ecy);
-    scale = ldexpf(1.f, F);
-    inv_scale = ldexpf(1.f, -F);
-    return true;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int c = 0; c < CB; ++c) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) m[c] = fmaxf(m[c], __shfl_xor_sync(0xffffffffu, m[c], o));
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < CB; ++c) red[warp * CB + c] = m[c];
+    }
+    __syncthreads();
+    bool any = false;
+    if (threadIdx.x < CB) {
+        const int c = threadIdx.x;
+        float ymax = 0.f;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) ymax = fmaxf(ymax, red[w * CB + c]);
+        int F = 0;
+        if (ymax > 0.f) {
+            any = true;
+            const float wsum = fmaxf(__int_as_float(bi.w), 1.0f);
+            int ey, ecy;
+            frexpf(ymax, &ey);                     // ymax < 2^ey
+            frexpf(ymax * wsum, &ecy);             // wsum*ymax < 2^ecy
+            F = max(-126, min(126, min(22 - ey, 30 - ecy)));
+        }
+        psc[c] = ldexpf(1.f, F);
+        psc[kMaxCB + c] = ldexpf(1.f, -F);
+    }
+    return __syncthreads_or(any) != 0;  // also: psc is visible to the block, red free again
 }
 
 // Add the integer planes of piece bi to the grid (vector atomics: the halos
 // of neighbouring tiles overlap) and return every plane read to zero.
 template <int CB, int R>
 __device__ __forceinline__ void flush_tile(float2 *__restrict__ G, int nc, int c0, int cb, const int4 bi,
-                                           const Geom &g, int *tile, float inv_scale)
+                                           const Geom &g, int *tile, const float *inv_scale)
 {
     constexpr int ps = IPlane<R>::PS;
     int ox, oy, oz;
@@ -750,8 +788,9 @@ __device__ __forceinline__ void flush_tile(float2 *__restrict__ G, int nc, int c
             t0[ps] = 0;
             t0[2 * ps] = 0;
             t0[3 * ps] = 0;
+            const float s0 = inv_scale[cc], s1 = inv_scale[cc + 1];
             atomicAdd(reinterpret_cast<float4 *>(&G[gidx * nc + c0 + cc]),
-                      make_float4(a * inv_scale, b * inv_scale, e * inv_scale, f * inv_scale));
+                      make_float4(a * s0, b * s0, e * s1, f * s1));
         });
     } else {
         for_tile_rows<CB>(g, ox, oy, oz, [&](int pt, int cc, size_t gidx) {
@@ -761,7 +800,8 @@ __device__ __forceinline__ void flush_tile(float2 *__restrict__ G, int nc, int c
             if ((a | b) == 0) return;
             t0[0] = 0;
             t0[ps] = 0;
-            atomicAdd(&G[gidx * nc + c0 + cc], make_float2(a * inv_scale, b * inv_scale));
+            const float s0 = inv_scale[cc];
+            atomicAdd(&G[gidx * nc + c0 + cc], make_float2(a * s0, b * s0));
         });
     }
 }
@@ -773,18 +813,19 @@ template <int CB, bool RADIAL, int R>
 __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
                                              const float4 *__restrict__ samples, const int4 bi, const Geom &g,
                                              const KBParams &kb, const CandPairs &cs, int *tile, float *red,
-                                             TapQueue2 *queues)
+                                             float *psc, TapQueue2 *queues)
 {
     constexpr int NP = Lanes<CB>::NP, CPS = Lanes<CB>::CPS;
     constexpr int ps = IPlane<R>::PS;
     const int Px = g.P[0];
     const int cb = min(CB, nc - c0);
     const int send = bi.y + bi.z;
-    float scale, inv_scale;
-    if (!piece_scale(ks, nc, c0, cb, bi, red, scale, inv_scale)) return;  // the tile stays zero
+    if (!piece_scale<CB>(ks, nc, c0, cb, bi, red, psc)) return;  // the tile stays zero
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const int q = lane / CPS, j = lane % CPS;
     const int c = CB >= 2 ? 2 * q : 0;
+    // this lane's coils' scales (c + 1 < CB whenever CB >= 2)
+    const float sa = psc[c], sb = CB >= 2 ? psc[c + 1] : 0.f;
     int *pl0 = tile + (size_t)(2 * c) * ps;  // re, im of coil c; then re, im of coil c+1
     const unsigned pl0_sa = (unsigned)__cvta_generic_to_shared(pl0);
     TapQueue2 &qu = queues[warp];
@@ -792,7 +833,7 @@ __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, floa
         const float2 *src = ks + (size_t)s * nc + c0;
         const float2 a = c < cb ? src[c] : make_float2(0.f, 0.f);
         const float2 b = (CB >= 2 && c + 1 < cb) ? src[c + 1] : make_float2(0.f, 0.f);
-        y = make_float4(a.x * scale, a.y * scale, b.x * scale, b.y * scale);
+        y = make_float4(a.x * sa, a.y * sa, b.x * sb, b.y * sb);
     };
     float4 rec_next = make_float4(0.f, 0.f, 0.f, 0.f), y_next = make_float4(0.f, 0.f, 0.f, 0.f);
     if (bi.y + warp < send) {
@@ -826,7 +867,7 @@ __device__ __forceinline__ void spread_piece(const float2 *__restrict__ ks, floa
         }
     }
     __syncthreads();
-    flush_tile<CB, R>(G, nc, c0, cb, bi, g, tile, inv_scale);
+    flush_tile<CB, R>(G, nc, c0, cb, bi, g, tile, psc + kMaxCB);
     __syncthreads();  // the tile is zero again
 }
 
@@ -851,7 +892,8 @@ k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
          Geom g, KBParams kb, const __grid_constant__ Cand cd)
 {
     extern __shared__ float4 smem4[];
-    __shared__ float red[33];
+    __shared__ float red[32 * CB];
+    __shared__ float psc[2 * kMaxCB];
     __shared__ TapQueue2 queues[kInterpThreads / 32];
     __shared__ int next;
     CandPairs cs;
@@ -861,7 +903,7 @@ k_spread(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
         __syncthreads();
         const int b = next;
         if (b >= nblocks) break;
-        spread_piece<CB, RADIAL, R>(ks, G, nc, c0, samples, blocks[b], g, kb, cs, tile, red, queues);
+        spread_piece<CB, RADIAL, R>(ks, G, nc, c0, samples, blocks[b], g, kb, cs, tile, red, psc, queues);
     }
 }
 
@@ -942,7 +984,7 @@ __device__ __forceinline__ bool gather_piece_tab(const float2 *__restrict__ G, f
                                                  const float *__restrict__ wsample,
                                                  const uint32_t *__restrict__ rows, const int2 *__restrict__ taps,
                                                  float2 *tile, const CUtensorMap *tmap, unsigned bar_sa,
-                                                 unsigned &phase)
+                                                 unsigned &phase, const InterpStatus &stat)
 {
     constexpr int CB = 8;
     const int lane = threadIdx.x & 31, lig = lane & 7;
@@ -962,7 +1004,7 @@ __device__ __forceinline__ bool gather_piece_tab(const float2 *__restrict__ G, f
     int2 e1 = nchk > 1 ? ld_tap(st + 8) : z2;
     int2 e2 = nchk > 2 ? ld_tap(st + 16) : z2;
     int2 e3 = nchk > 3 ? ld_tap(st + 24) : z2;
-    if (!stage_tile<CB>(G, nc, c0, bi, g, tile, tmap, bar_sa, phase)) return false;
+    if (!stage_tile<CB>(G, nc, c0, bi, g, tile, tmap, bar_sa, phase, stat)) return false;
     const int cb = min(CB, nc - c0);
     const int rot = lig & 3, rot16 = rot << 4;
     float2 acc[CB];
@@ -1041,7 +1083,7 @@ __global__ void __launch_bounds__(kInterpThreads)
 k_gather_tab(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int c0,
              const int4 *__restrict__ blocks, int nblocks, int *__restrict__ work, Geom g, float scale,
              const float *__restrict__ wsample, const uint32_t *__restrict__ rows, const int2 *__restrict__ taps,
-             const __grid_constant__ CUtensorMap tmap, int use_tma)
+             const __grid_constant__ CUtensorMap tmap, int use_tma, InterpStatus st)
 {
     extern __shared__ float4 smem4[];
     __shared__ unsigned long long bar;
@@ -1057,7 +1099,7 @@ k_gather_tab(const float2 *__restrict__ G, float2 *__restrict__ ks, int nc, int 
         const int b = next;
         if (b >= nblocks) break;
         if (!gather_piece_tab<R>(G, ks, nc, c0, blocks[b], g, scale, wsample, rows, taps, tile,
-                                 use_tma ? &tmap : nullptr, bar_sa, phase))
+                                 use_tma ? &tmap : nullptr, bar_sa, phase, st))
             return;
     }
 }
@@ -1276,7 +1318,7 @@ k_gather_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ ta
         const CUtensorMap *tm = (b.tmap_ok >> lw) & 1 ? &b.tmaps[lw] : nullptr;
         // the kernel weights come from the parameter bank (shared by the batch)
         if (!gather_piece<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, kb, b.scale,
-                                         b.wsample, m.cs, m.tile, tm, m.bar_sa, phase))
+                                         b.wsample, m.cs, m.tile, tm, m.bar_sa, phase, b.status))
             return;
     }
 }
@@ -1306,7 +1348,7 @@ k_gather_batch_tab(const BatchInterp *__restrict__ vols, const int4 *__restrict_
         const BatchInterp &b = vols[e.x];
         const CUtensorMap *tm = (b.tmap_ok >> 3) & 1 ? &b.tmaps[3] : nullptr;
         if (!gather_piece_tab<R>(b.in, b.out, b.nc, e.z, b.blocks[e.y], b.g, b.scale, b.wsample, b.tap_rows,
-                                 b.tap_ent, tile, tm, bar_sa, phase))
+                                 b.tap_ent, tile, tm, bar_sa, phase, b.status))
             return;
     }
 }
@@ -1317,7 +1359,8 @@ k_spread_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ ta
                int *__restrict__ work, KBParams kb)
 {
     extern __shared__ float4 smem4[];
-    __shared__ float red[33];
+    __shared__ float red[32 * CB];
+    __shared__ float psc[2 * kMaxCB];
     __shared__ TapQueue2 queues[kInterpThreads / 32];
     __shared__ int next;
     CandPairs cs;
@@ -1330,7 +1373,7 @@ k_spread_batch(const BatchInterp *__restrict__ vols, const int4 *__restrict__ ta
         const int4 e = table[t];
         const BatchInterp &b = vols[e.x];
         spread_piece<CB, RADIAL, R>(b.in, b.out, b.nc, e.z, b.samples, b.blocks[e.y], b.g, kb, cs, tile, red,
-                                    queues);
+                                    psc, queues);
     }
 }
 
@@ -1433,15 +1476,18 @@ bool encode_gather_map(const nufft3d_plan *p, const float2 *G, int nc, int cb, C
     }
 }
 
-int interp_check_error()
+int plan_check_status(nufft3d_plan *p, cudaStream_t s)
 {
-    unsigned v = 0;
-    if (cudaMemcpyFromSymbol(&v, g_interp_err, sizeof(v)) != cudaSuccess) return NUFFT3D_ERR_CUDA;
+    int v = 0;
+    int *flag = p->work + kWorkStatus;
+    NUFFT_CUDA_TRY(cudaMemcpyAsync(&v, flag, sizeof(v), cudaMemcpyDeviceToHost, s));
+    NUFFT_CUDA_TRY(cudaMemsetAsync(flag, 0, sizeof(int), s));
+    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
     if (!v) return NUFFT3D_SUCCESS;
-    const unsigned zero = 0;
-    cudaMemcpyToSymbol(g_interp_err, &zero, sizeof(zero));
     return fail(NUFFT3D_ERR_TIMEOUT, "a tile copy in the interpolation did not complete in time");
 }
+
+InterpStatus plan_status(const nufft3d_plan *p) { return InterpStatus{p->work + kWorkStatus, p->wait_polls}; }
 
 template <int CB, bool RADIAL, int R>
 static int gather_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, int c0, float scale,
@@ -1456,7 +1502,7 @@ static int gather_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, int c0
     const int64_t grid = std::min<int64_t>(p->n_blocks, p->sm_count);
     k_gather<CB, RADIAL, R><<<(unsigned)grid, kInterpThreads, smem, s>>>(
         G, ks, nc, c0, p->samples, p->blocks, (int)p->n_blocks, p->work, p->geom, p->kb, scale, ws, cand_of(p), m,
-        use_tma);
+        use_tma, plan_status(p));
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }
@@ -1487,7 +1533,7 @@ static int gather_tab_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, in
     const int64_t grid = std::min<int64_t>(p->n_blocks, p->sm_count);
     k_gather_tab<R><<<(unsigned)grid, kInterpThreads, smem, s>>>(G, ks, nc, c0, p->blocks, (int)p->n_blocks,
                                                                  p->work, p->geom, scale, ws, p->tap_rows,
-                                                                 p->tap_ent, m, use_tma);
+                                                                 p->tap_ent, m, use_tma, plan_status(p));
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
 }
@@ -1587,7 +1633,7 @@ int launch_tap_count(nufft3d_plan *p, uint32_t *rows, cudaStream_t s)
 int launch_tap_fill(nufft3d_plan *p, const uint32_t *rows, int2 *taps, cudaStream_t s)
 {
     if (p->nnz == 0) return NUFFT3D_SUCCESS;
-    int *err = p->work + 2;  // the plan's own flag (plans may be built concurrently)
+    int *err = p->work + kWorkTapFill;  // the plan's own flag (plans may be built concurrently)
     NUFFT_CUDA_TRY(cudaMemsetAsync(err, 0, sizeof(int), s));
     int cap = 0;
     for (int q = 0; q < 8; ++q) cap = std::max(cap, p->cand_desc.cnt[q]);

@@ -733,8 +733,7 @@ static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts
         const int iters = o.density_iters > 0 ? o.density_iters : (o.density_iters == 0 ? 20 : 0);
         NUFFT_TRY(run_density(p, iters, s));
     }
-    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
-    return NUFFT3D_SUCCESS;
+    return plan_check_status(p, s);
 }
 
 int refresh_density_orig(nufft3d_plan *p, cudaStream_t s)
@@ -763,6 +762,7 @@ extern "C" int nufft3d_opts_default(nufft3d_opts *o)
     o->d = nullptr;
     o->density_iters = 20;
     o->tap_table = -1;
+    o->wait_polls = kDefaultWaitPolls;
     return NUFFT3D_SUCCESS;
 }
 
@@ -810,6 +810,7 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
     for (int a = 0; a < 3; ++a) K[a] = 2 * (int)std::ceil(N[a] * o.u / 2);
     if (is2d) K[2] = 1;
     if ((double)K[0] * K[1] * K[2] >= 2147483647.0) return fail(NUFFT3D_ERR_SIZE, "N or u too large");
+    if (o.wait_polls < 0) return fail(NUFFT3D_ERR_ARG, "wait_polls must be nonnegative");
 
     int dev = o.device;
     if (dev < 0) {
@@ -871,7 +872,10 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
         delete p;
         return fail(NUFFT3D_ERR_CUDA, "cudaStreamCreate failed");
     }
+    p->wait_polls = o.wait_polls;
     int st = dmalloc(&p->work, 16, nullptr);  // per handle: handles may run concurrently
+    if (st == NUFFT3D_SUCCESS && cudaMemset(p->work, 0, 16 * sizeof(int)) != cudaSuccess)
+        st = fail(NUFFT3D_ERR_CUDA, "cannot clear the plan's work buffer");
     if (st == NUFFT3D_SUCCESS) st = build_plan(p, om, o);
     if (st != NUFFT3D_SUCCESS) {
         std::string msg = nufft3d_last_error();
@@ -939,8 +943,10 @@ extern "C" int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **out)
         delete p;
         return fail(NUFFT3D_ERR_CUDA, "cudaStreamCreate failed");
     }
-    if (dmalloc(&p->work, 16, nullptr) != NUFFT3D_SUCCESS) {
-        std::string msg = nufft3d_last_error();
+    p->wait_polls = src->wait_polls;
+    if (dmalloc(&p->work, 16, nullptr) != NUFFT3D_SUCCESS || cudaMemset(p->work, 0, 16 * sizeof(int)) != cudaSuccess) {
+        std::string msg = p->work ? std::string("cannot clear the handle's work buffer") : nufft3d_last_error();
+        if (p->work) cudaFree(p->work);
         cudaStreamDestroy(p->own_stream);
         p->tables.reset();
         delete p;

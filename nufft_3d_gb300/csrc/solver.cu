@@ -748,8 +748,7 @@ static int inverse_host(nufft3d_plan *p, const float *raw, float *x, int nc, int
         NUFFT_TRY(run_inverse(p, (const float2 *)base, (float2 *)h.out, nc, maxit, damp, Wd, solver, tol,
                               iters_host, s, warm));
     NUFFT_CUDA_TRY(cudaMemcpyAsync(x, h.out, bx, cudaMemcpyDeviceToHost, s));
-    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
-    NUFFT_TRY(interp_check_error());
+    NUFFT_TRY(plan_check_status(p, s));
     return NUFFT3D_SUCCESS;
 }
 

@@ -42,7 +42,8 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
     """obj = nufft_3d(om, N, name, value, ...)"""
 
     def __init__(self, om, N=None, *varargin, device=None, tile=None, coils_per_pass=None,
-                 samples_per_block=None, density_iters=20, verbose=False, tap_table=None, **kw):
+                 samples_per_block=None, density_iters=20, verbose=False, tap_table=None, wait_polls=None,
+                 **kw):
         L = _lib.load()
         # name/value pairs (nufft_3d.m:71-76)
         if len(varargin) % 2:
@@ -93,6 +94,8 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
         opts.verbose = int(bool(verbose))
         if tap_table is not None:  # True/1 build, False/0 on the fly, -1 auto (default)
             opts.tap_table = int(tap_table)
+        if wait_polls is not None:  # polls of each bounded wait (0: give up at once)
+            opts.wait_polls = int(wait_polls)
         dbuf = None
         if pairs.get("d") is not None:
             dbuf = np.ascontiguousarray(np.asarray(pairs["d"], dtype=np.float32).reshape(-1))
@@ -152,6 +155,17 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
         b = ctypes.c_int64()
         _lib.check(self._L.nufft3d_plan_footprint(self.plan, int(nc), int(bool(with_solver)), ctypes.byref(b)))
         return int(b.value)
+
+    def check_status(self, stream=None):
+        """Raises NufftError (NUFFT3D_ERR_TIMEOUT) if a bounded wait expired in
+        device-pointer calls queued on `stream` (a torch.cuda.Stream, a raw
+        handle, or None for torch's current stream) since the last check;
+        synchronises that stream (nufft3d_check_status)."""
+        if stream is None:
+            import torch
+            stream = torch.cuda.current_stream()
+        h = getattr(stream, "cuda_stream", stream)
+        _lib.check(self._L.nufft3d_check_status(self.plan, ctypes.c_void_p(h)))
 
     @property
     def plan(self):

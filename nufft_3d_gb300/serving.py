@@ -96,6 +96,7 @@ class ReconServer:
         self.stop = False
         self.errors = []
         self.handle = [None] * slots      # per slot: (key, shared handle) kept between batches
+        self.busy = [False] * slots       # per slot: a batch is between admission and finish
         self.slot_res = [(None, 0)] * slots  # per slot: (key, bytes reserved for its handle)
         self.workers = [threading.Thread(target=self._worker, args=(i,), daemon=True) for i in range(slots)]
         for w in self.workers:
@@ -162,18 +163,43 @@ class ReconServer:
                 coils += r.nc
         return batch, coils
 
+    def _release_slot(self, slot):
+        """Under the lock: close the slot's idle handle and credit back the
+        work-buffer bytes reserved for it.  Its trajectory's tables stay with
+        the cached base plan (if any), whose bytes are counted separately."""
+        cur = self.handle[slot]
+        if cur is not None:
+            cur[1].close()
+            self.handle[slot] = None
+        self.used -= self.slot_res[slot][1]
+        self.slot_res[slot] = (None, 0)
+
     def _evict_for(self, need, slot, keep):
-        # the requesting slot's own handle does not pin its key: the slot
-        # closes that handle before it runs the new batch (the tables go with
-        # the last handle); the key the request needs stays
-        for key in list(self.cache):
-            if self.used + need <= self.budget:
-                break
-            e = self.cache[key]
-            if key != keep and e["users"] == 0 and all(r[0] != key for i, r in enumerate(self.slot_res) if i != slot):
-                e["plan"].close()
-                self.used -= e["bytes"]
-                del self.cache[key]
+        """Under the lock: free memory for `need` more bytes.  First cached
+        trajectories that nothing uses (tables that no handle holds are freed
+        with their base plan); then the handles of idle slots, which pin their
+        trajectory and hold work buffers, and the trajectories they released.
+        The requesting slot has already closed a handle on another key; the
+        key the request needs stays."""
+        def evict_idle_plans():
+            for key in list(self.cache):
+                if self.used + need <= self.budget:
+                    return
+                e = self.cache[key]
+                if (key != keep and e["users"] == 0 and e["plan"] is not None
+                        and all(r[0] != key for i, r in enumerate(self.slot_res) if i != slot)):
+                    e["plan"].close()
+                    self.used -= e["bytes"]
+                    del self.cache[key]
+
+        evict_idle_plans()
+        if self.used + need <= self.budget:
+            return
+        for i in range(len(self.slot_res)):
+            # an idle slot is waiting in _admit under this lock: its handle is unused
+            if i != slot and not self.busy[i] and self.slot_res[i][0] is not None:
+                self._release_slot(i)
+        evict_idle_plans()
 
     def _admit(self, slot):
         """Under the lock: pick a batch whose memory fits, reserve it for `slot`."""
@@ -182,20 +208,27 @@ class ReconServer:
         batch, coils = self._take_batch()
         req0 = batch[0][0]
         work = self._work_bytes(req0, coils)
+        if self.slot_res[slot][0] not in (None, req0.key):
+            # the slot changes trajectory: close its old handle now, so the
+            # bytes credited back are free before anything new is allocated
+            self._release_slot(slot)
         rkey, rbytes = self.slot_res[slot]
         if rkey == req0.key:
             extra = max(0, work - rbytes)
             new_res = max(work, rbytes)
         else:
-            extra = work - rbytes      # the slot's old handle is closed
+            extra = work
             new_res = work
         new_plan = req0.key not in self.cache
         pbytes = self._plan_bytes_estimate(req0) if new_plan else 0
         need = extra + pbytes
         if self.used + need > self.budget:
             self._evict_for(need, slot, req0.key)
-        if self.used + need > self.budget and any(e["users"] for e in self.cache.values()):
-            return None           # wait for memory to be released by running work
+        if self.used + need > self.budget:
+            if any(self.busy):
+                return None           # wait for memory to be released by running work
+            raise MemoryError("reconstruction needs %.2f GiB of device memory beyond the %.2f GiB held; "
+                              "budget %.2f GiB" % (_gib(need), _gib(self.used), _gib(self.budget)))
         for item in batch:
             self.queue.remove(item)
         if new_plan:
@@ -205,6 +238,7 @@ class ReconServer:
         entry["users"] += 1
         self.used += need
         self.slot_res[slot] = (req0.key, new_res)
+        self.busy[slot] = True
         return batch, coils, entry, new_plan
 
     def _worker(self, slot):
@@ -231,19 +265,7 @@ class ReconServer:
             req0 = batch[0][0]
             t0 = time.perf_counter()
             try:
-                if new_plan:
-                    entry["plan"] = nufft_3d(req0.om, req0.N, device=self.device, **req0.opts)
-                    entry["ready"].set()
-                else:
-                    entry["ready"].wait()
-                    if entry["plan"] is None:
-                        raise RuntimeError("plan construction failed in another slot")
-                cur = self.handle[slot]
-                if cur is None or cur[0] != req0.key:
-                    if cur is not None:
-                        cur[1].close()
-                    self.handle[slot] = (req0.key, entry["plan"].share())
-                h = self.handle[slot][1]
+                h = self._acquire_handle(slot, req0, entry, new_plan)
                 raws = [r.raw.reshape(r.raw.shape[0], -1) for r, _ in batch]
                 raw = np.concatenate(raws, axis=1) if len(raws) > 1 else raws[0]
                 im = h.iNUFT(raw, req0.maxit, req0.damp, solver=req0.solver, tol=req0.tol)
@@ -263,19 +285,44 @@ class ReconServer:
                     if not fut.done():
                         fut.set_exception(e)
             finally:
-                with self.cv:
-                    entry["users"] -= 1
-                    if entry["plan"] is None and entry["users"] == 0:
-                        self.used -= entry["bytes"]
-                        self.cache.pop(req0.key, None)
-                    while len(self.cache) > self.cache_size:
-                        k, e = next(iter(self.cache.items()))
-                        if e["users"] or any(r[0] == k for r in self.slot_res):
-                            break
-                        e["plan"].close()
-                        self.used -= e["bytes"]
-                        del self.cache[k]
-                    self.cv.notify_all()
+                self._finish(slot, req0.key, entry)
+
+    def _make_plan(self, req):
+        return nufft_3d(req.om, req.N, device=self.device, **req.opts)
+
+    def _acquire_handle(self, slot, req0, entry, new_plan):
+        """The slot's handle on req0's trajectory, building the base plan if
+        this batch admitted a new one.  A handle on another trajectory was
+        closed by _admit, so old and new tables are never both held here."""
+        if new_plan:
+            entry["plan"] = self._make_plan(req0)
+            entry["ready"].set()
+        else:
+            entry["ready"].wait()
+            if entry["plan"] is None:
+                raise RuntimeError("plan construction failed in another slot")
+        cur = self.handle[slot]
+        if cur is None or cur[0] != req0.key:
+            if cur is not None:  # not reached: _admit releases a handle on another key
+                cur[1].close()
+            self.handle[slot] = (req0.key, entry["plan"].share())
+        return self.handle[slot][1]
+
+    def _finish(self, slot, key, entry):
+        with self.cv:
+            self.busy[slot] = False
+            entry["users"] -= 1
+            if entry["plan"] is None and entry["users"] == 0:
+                self.used -= entry["bytes"]
+                self.cache.pop(key, None)
+            while len(self.cache) > self.cache_size:
+                k, e = next(iter(self.cache.items()))
+                if e["users"] or any(r[0] == k for r in self.slot_res):
+                    break
+                e["plan"].close()
+                self.used -= e["bytes"]
+                del self.cache[k]
+            self.cv.notify_all()
 
 
 def run_served(requests, slots=4, hbm_budget=None, device=0, max_batch_coils=16, t0=None):

@@ -33,7 +33,8 @@ def test_opts_struct_layout_matches_defaults():
     o = _lib.Opts()
     assert L.nufft3d_opts_default(ctypes.byref(o)) == 0
     assert (o.J, o.u, o.alpha, o.radial, o.gpu, o.density_iters) == (4.0, 2.0, 0.0, 1, 1, 20)
-    assert o.tap_table == -1  # the stored H is built when it fits (last field: the layout matches the header)
+    assert o.tap_table == -1  # the stored H is built when it fits
+    assert o.wait_polls == 1 << 22  # last field: the layout matches the header
 
 
 def test_header_struct_fields_match_ctypes():
@@ -75,6 +76,7 @@ def _create(om, N, **kw):
     ({}, [16, 15, 16], _lib.ERR_ARG, "even integer"),
     (dict(gpu=0), 16, _lib.ERR_UNSUPPORTED, "CPU"),         # no CPU fallback
     (dict(J=9.0), 16, _lib.ERR_UNSUPPORTED, "J"),
+    (dict(wait_polls=-1), 16, _lib.ERR_ARG, "wait_polls"),
 ])
 def test_invalid_arguments_rejected(kw, N, code, msg):
     om = np.random.default_rng(0).uniform(-4, 4, (3, 50))
@@ -119,3 +121,8 @@ def test_solver_entry_points_check_arguments_without_a_device():
     assert L.nufft3d_inverse_phase(None, buf, buf, 1, 5, 0.1, 0.5, None, 0.0, its, None) == _lib.ERR_ARG
     assert L.nufft3d_inverse_phase_host(None, buf, buf, 1, 5, 0.1, -1.0, None, 0.0, its) == _lib.ERR_ARG
     assert "lambda" in _lib.last_error()
+
+
+def test_check_status_rejects_null_plan():
+    L = _lib.load()
+    assert L.nufft3d_check_status(None, None) == _lib.ERR_ARG

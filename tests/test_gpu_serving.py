@@ -106,3 +106,32 @@ def test_served_vs_plain_stream(cuda):
     s = summarize(served, wall_s)
     p = summarize(plain, wall_p)
     assert s["requests"] == p["requests"] == 8
+
+
+def test_low_and_high_gain_requests_merged_match_alone(cuda):
+    """Two requests on one trajectory, one with 1e4 times the gain of the
+    other, queued together so the server merges them into one 4-coil solve:
+    each result equals the same request solved alone to rel L2 1e-5 (each
+    coil keeps its own fixed-point scale in the spread)."""
+    lo = make_request(32, 700, 2, 31, traj_seed=5)
+    hi = make_request(32, 700, 2, 32, traj_seed=5)
+    lo.raw = (lo.raw * 1e-4).astype(np.complex64)
+    hi.raw = (hi.raw * 1e0).astype(np.complex64)
+    assert lo.key == hi.key
+    alone = []
+    for r in (lo, hi):
+        obj = nufft_3d(r.om, r.N, **r.opts)
+        alone.append(obj.iNUFT(r.raw, r.maxit, r.damp, solver=r.solver, tol=r.tol))
+        obj.close()
+    srv = ReconServer(slots=1, max_batch_coils=8)
+    srv.cv.acquire()          # queue both before the worker can take the first
+    try:
+        futs = [srv.submit(r) for r in (lo, hi)]
+    finally:
+        srv.cv.release()
+    done = [f.result(timeout=120) for f in futs]
+    srv.close()
+    assert not srv.errors
+    assert done[0].t_start == done[1].t_start  # one merged solve
+    for r, a in zip(done, alone):
+        assert rel(r.result, a) < 1e-5, rel(r.result, a)

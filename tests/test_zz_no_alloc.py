@@ -16,25 +16,42 @@ pytestmark = pytest.mark.gpu
 TOL_OP = 1e-5
 
 
-def test_forward_noalloc_matches_forward_twice(cuda):
+def _traj(N, two_d):
+    from nufft_3d_gb300 import synth
+    if not two_d:
+        return synth.koosh_ball(N, N, 600)
+    rng = np.random.default_rng(9)
+    return np.vstack([rng.uniform(-N / 2, N / 2 - 1, (2, 3000)), np.zeros((1, 3000))])
+
+
+@pytest.mark.parametrize("N,nc,two_d", [
+    (24, 3, False),   # coil passes of 2 and 1: the kernel-evaluating gather
+    (24, 8, False),   # one 8-coil pass: the stored-H gather, bulk tile copies on the carved grid
+    (48, 8, True),    # 2-D: the grid aliases the y-pass buffer
+])
+def test_forward_noalloc_matches_forward_twice(cuda, N, nc, two_d):
     torch = cuda
-    from nufft_3d_gb300 import _lib, nufft_3d, synth
+    from nufft_3d_gb300 import _lib, nufft_3d
 
     L = _lib.load()
-    N, nc = 24, 3
-    om = synth.koosh_ball(N, 24, 600)
-    obj = nufft_3d(om, N, "J", 6, density_iters=0)
+    om = _traj(N, two_d)
+    obj = nufft_3d(om, N, "J", 6, density_iters=0, tap_table=1)
+    if nc == 8:
+        assert obj.tap_table_bytes > 0
+    if two_d:
+        assert list(obj.N) == [N, N, 1]
+    shape = (nc,) + tuple(int(v) for v in obj.N[::-1])
     stream = torch.cuda.current_stream()
     sp = ctypes.c_void_p(stream.cuda_stream)
     g = torch.Generator(device="cuda").manual_seed(0)
     outs = []
     for call in range(2):
-        x = torch.randn((nc, N, N, N), dtype=torch.complex64, device="cuda", generator=g)
+        x = torch.randn(shape, dtype=torch.complex64, device="cuda", generator=g)
         ref = torch.empty((nc, obj.M), dtype=torch.complex64, device="cuda")
         out = torch.full((nc, obj.M), float("nan"), dtype=torch.complex64, device="cuda")
         _lib.check(L.nufft3d_forward(obj.plan, x.data_ptr(), ref.data_ptr(), nc, sp))
         _lib.check(L.nufft3d_forward_noalloc(obj.plan, x.data_ptr(), out.data_ptr(), nc, sp))
-        torch.cuda.synchronize()
+        _lib.check(L.nufft3d_check_status(obj.plan, sp))  # no bounded wait expired
         err = float((out - ref).abs().norm() / ref.abs().norm())
         assert err < TOL_OP, (call, err)
         outs.append(out)
