@@ -3,7 +3,9 @@
 %   obj = nufft_3d(om, N, 'J', 6, 'u', 2, 'radial', 1, ...)
 %   k   = obj.fNUFT(x);        x [N1 N2 N3 nc]  -> k [M nc]
 %   x   = obj.aNUFT(k);        k [M nc]         -> x [N1 N2 N3 nc]
-%   im  = obj.iNUFT(raw, maxit, damp, W);
+%   im  = obj.iNUFT(raw, maxit, damp, W, constraint, lambda);
+%   damp = obj.discrep(data, stddev);
+%   k   = obj * x;  x = obj' * k   (mtimes / ctranspose)
 %
 % Same constructor name/value pairs, read-only properties and method names as
 % the reference class (nufft_3d.m:26-43, 54-251).  The sparse matrix H is not
@@ -28,6 +30,8 @@ classdef nufft_3d < handle
     properties (Access = private, Hidden = true)
         plan = uint64(0)            % libnufft3d plan handle
         M(1,1) double = 0           % number of samples
+        adjoint(1,1) logical = false % obj' (ctranspose): * applies aNUFT
+        owner = []                  % the object whose plan a transposed view borrows
     end
 
     methods
@@ -71,10 +75,11 @@ classdef nufft_3d < handle
         end
 
         function delete(obj)
-            if obj.plan ~= 0
+            % a transposed view borrows its owner's plan
+            if obj.plan ~= 0 && isempty(obj.owner)
                 nufft3d_mex('destroy', obj.plan);
-                obj.plan = uint64(0);
             end
+            obj.plan = uint64(0);
         end
     end
 

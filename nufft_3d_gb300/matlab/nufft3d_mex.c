@@ -12,6 +12,12 @@
  *   [x, it]  = nufft3d_mex('inverse', h, raw, maxit, damp, W, solver, tol)
  *              nufft3d_inverse_host; W [] or single [M]; solver 'minres'|'cg'
  *              it = iterations per coil
+ *   [x, it]  = nufft3d_mex('inverse_x0', h, raw, x0, maxit, damp, W, solver, tol)
+ *              nufft3d_inverse_x0_host: the same solve started from x0
+ *              (complex single [N1 N2 N3 nc]), as discrep.m warm-starts it
+ *   [x, it]  = nufft3d_mex('inverse_phase', h, raw, maxit, damp, lambda, W, tol)
+ *              nufft3d_inverse_phase_host: iNUFT with 'phase-constraint'
+ *              (iNUFT.m:140-168); it = iterations of the constrained solve
  *              nufft3d_mex('density', h, maxit)     nufft3d_density
  *   s        = nufft3d_mex('info', h)               nufft3d_plan_info
  *   U        = nufft3d_mex('deap', h)               nufft3d_get_deap
@@ -143,36 +149,83 @@ static void cmd_adjoint(mxArray **plhs, const mxArray **prhs)
     CALL(nufft3d_adjoint_host(p, (const float *)k, (float *)mxGetComplexSingles(plhs[0]), nc));
 }
 
-static void cmd_inverse(int nlhs, mxArray **plhs, int nrhs, const mxArray **prhs)
+static const float *weights_or_null(const mxArray *a, int64_t M)
 {
-    if (nrhs < 8) mexErrMsgIdAndTxt("nufft3d:args", "inverse needs h, raw, maxit, damp, W, solver, tol");
+    if (mxIsEmpty(a)) return NULL;
+    if (!mxIsSingle(a) || mxIsComplex(a) || (int64_t)mxGetNumberOfElements(a) != M)
+        mexErrMsgIdAndTxt("nufft3d:args", "W must be [] or real single with %lld elements", (long long)M);
+    return mxGetSingles(a);
+}
+
+static int solver_of(const mxArray *a)
+{
+    char solver[16] = {0};
+    if (mxGetString(a, solver, sizeof solver) != 0)
+        mexErrMsgIdAndTxt("nufft3d:args", "solver must be 'minres' or 'cg'");
+    const int sol = strcmp(solver, "cg") == 0 ? NUFFT3D_SOLVER_CG : NUFFT3D_SOLVER_MINRES;
+    if (sol == NUFFT3D_SOLVER_MINRES && strcmp(solver, "minres") != 0)
+        mexErrMsgIdAndTxt("nufft3d:args", "solver must be 'minres' or 'cg'");
+    return sol;
+}
+
+static void iters_out(int nlhs, mxArray **plhs, mxArray *it)
+{
+    if (nlhs > 1)
+        plhs[1] = it;
+    else
+        mxDestroyArray(it);
+}
+
+/* [x, it] = inverse(h, raw, maxit, damp, W, solver, tol) and, with warm = 1,
+ * inverse_x0(h, raw, x0, maxit, damp, W, solver, tol) */
+static void cmd_inverse(int nlhs, mxArray **plhs, int nrhs, const mxArray **prhs, int warm)
+{
+    const int a = warm ? 1 : 0;  /* x0 shifts the later arguments by one */
+    if (nrhs < 8 + a)
+        mexErrMsgIdAndTxt("nufft3d:args", warm ? "inverse_x0 needs h, raw, x0, maxit, damp, W, solver, tol"
+                                               : "inverse needs h, raw, maxit, damp, W, solver, tol");
+    nufft3d_plan *p = get_plan(prhs[1]);
+    const nufft3d_info in = plan_info(p);
+    const int nc = coils_of(prhs[2], in.M, "raw");
+    const mxComplexSingle *raw = complex_single(prhs[2], "raw");
+    const int maxit = (int)mxGetScalar(prhs[3 + a]);
+    const double damp = mxGetScalar(prhs[4 + a]);
+    const float *W = weights_or_null(prhs[5 + a], in.M);
+    const int sol = solver_of(prhs[6 + a]);
+    const double tol = mxGetScalar(prhs[7 + a]);
+    plhs[0] = complex_out(0, nc, in.N);
+    float *x = (float *)mxGetComplexSingles(plhs[0]);
+    mxArray *it = mxCreateNumericMatrix(1, (mwSize)nc, mxINT32_CLASS, mxREAL);
+    if (warm) {
+        const int64_t nvox = (int64_t)in.N[0] * in.N[1] * in.N[2];
+        if (coils_of(prhs[3], nvox, "x0") != nc)
+            mexErrMsgIdAndTxt("nufft3d:size", "x0 must have as many coils as raw");
+        memcpy(x, complex_single(prhs[3], "x0"), sizeof(mxComplexSingle) * (size_t)(nvox * nc));
+        CALL(nufft3d_inverse_x0_host(p, (const float *)raw, x, nc, maxit, damp, W, sol, tol, mxGetInt32s(it)));
+    } else {
+        CALL(nufft3d_inverse_host(p, (const float *)raw, x, nc, maxit, damp, W, sol, tol, mxGetInt32s(it)));
+    }
+    iters_out(nlhs, plhs, it);
+}
+
+/* [x, it] = inverse_phase(h, raw, maxit, damp, lambda, W, tol) */
+static void cmd_inverse_phase(int nlhs, mxArray **plhs, int nrhs, const mxArray **prhs)
+{
+    if (nrhs < 8) mexErrMsgIdAndTxt("nufft3d:args", "inverse_phase needs h, raw, maxit, damp, lambda, W, tol");
     nufft3d_plan *p = get_plan(prhs[1]);
     const nufft3d_info in = plan_info(p);
     const int nc = coils_of(prhs[2], in.M, "raw");
     const mxComplexSingle *raw = complex_single(prhs[2], "raw");
     const int maxit = (int)mxGetScalar(prhs[3]);
     const double damp = mxGetScalar(prhs[4]);
-    const float *W = NULL;
-    if (!mxIsEmpty(prhs[5])) {
-        if (!mxIsSingle(prhs[5]) || mxIsComplex(prhs[5]) || (int64_t)mxGetNumberOfElements(prhs[5]) != in.M)
-            mexErrMsgIdAndTxt("nufft3d:args", "W must be [] or real single with %lld elements", (long long)in.M);
-        W = mxGetSingles(prhs[5]);
-    }
-    char solver[16] = {0};
-    if (mxGetString(prhs[6], solver, sizeof solver) != 0)
-        mexErrMsgIdAndTxt("nufft3d:args", "solver must be 'minres' or 'cg'");
-    const int sol = strcmp(solver, "cg") == 0 ? NUFFT3D_SOLVER_CG : NUFFT3D_SOLVER_MINRES;
-    if (sol == NUFFT3D_SOLVER_MINRES && strcmp(solver, "minres") != 0)
-        mexErrMsgIdAndTxt("nufft3d:args", "solver must be 'minres' or 'cg'");
+    const double lambda = mxGetScalar(prhs[5]);
+    const float *W = weights_or_null(prhs[6], in.M);
     const double tol = mxGetScalar(prhs[7]);
     plhs[0] = complex_out(0, nc, in.N);
     mxArray *it = mxCreateNumericMatrix(1, (mwSize)nc, mxINT32_CLASS, mxREAL);
-    CALL(nufft3d_inverse_host(p, (const float *)raw, (float *)mxGetComplexSingles(plhs[0]), nc, maxit, damp, W,
-                              sol, tol, mxGetInt32s(it)));
-    if (nlhs > 1)
-        plhs[1] = it;
-    else
-        mxDestroyArray(it);
+    CALL(nufft3d_inverse_phase_host(p, (const float *)raw, (float *)mxGetComplexSingles(plhs[0]), nc, maxit, damp,
+                                    lambda, W, tol, mxGetInt32s(it)));
+    iters_out(nlhs, plhs, it);
 }
 
 static void cmd_info(mxArray **plhs, const mxArray **prhs)
@@ -214,7 +267,11 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
     } else if (strcmp(cmd, "adjoint") == 0 && nrhs >= 3) {
         cmd_adjoint(plhs, prhs);
     } else if (strcmp(cmd, "inverse") == 0) {
-        cmd_inverse(nlhs, plhs, nrhs, prhs);
+        cmd_inverse(nlhs, plhs, nrhs, prhs, 0);
+    } else if (strcmp(cmd, "inverse_x0") == 0) {
+        cmd_inverse(nlhs, plhs, nrhs, prhs, 1);
+    } else if (strcmp(cmd, "inverse_phase") == 0) {
+        cmd_inverse_phase(nlhs, plhs, nrhs, prhs);
     } else if (strcmp(cmd, "density") == 0 && nrhs >= 3) {
         CALL(nufft3d_density(get_plan(prhs[1]), (int)mxGetScalar(prhs[2])));
     } else if (strcmp(cmd, "info") == 0) {

@@ -10,9 +10,9 @@ either machine and the reference ships no golden vectors or known-answer
 tests.  This restatement is therefore checked against independent known
 answers instead (A&S/NR bounds of I0 against ``scipy.special.i0``, the
 closed-form Beatty alpha, the analytic Lewitt deapodization that the reference
-keeps disabled in ``deap.m:73-128``, the Cartesian full-grid case of
+keeps disabled in ``deap.m:38-95``, the Cartesian full-grid case of
 ``test_nufft3d.m:46-52`` against a plain FFT, the exact adjoint identity and
-diag(Q'Q) ~ 1 from ``density.m:182-207``), see ``tests/test_oracle.py``.
+diag(Q'Q) ~ 1 from ``density.m:44-82``), see ``tests/test_oracle.py``.
 
 Conventions follow the reference file by file (paths relative to the
 reference project root):

@@ -19,6 +19,7 @@ import numpy as np
 import pytest
 
 from nufft_3d_gb300 import _lib, nufft_3d, synth
+from oracle.cpu_bench import adjoint_per_coil, forward_per_coil
 from oracle.nufft_ref import NufftRef
 
 pytestmark = pytest.mark.gpu
@@ -75,31 +76,6 @@ def test_coils_of_different_gain_in_one_pass(cuda, nc):
     assert rel(a1[..., 0], a[..., 1]) < 1e-6
 
 
-def _oracle_forward_per_coil(ref, x):
-    """fNUFT of an (N1,N2,N3,nc) image, coil by coil through fft3_pad (bounded
-    host memory), one matrix-free H product for all coils."""
-    import math
-    N, K = ref.N, ref.K
-    nc = x.shape[3]
-    G = np.empty((int(np.prod(K)), nc), dtype=np.complex128)
-    for c in range(nc):
-        k = np.asarray(x[..., c:c + 1], dtype=np.complex128) * ref.U[..., None]
-        G[:, c] = ref.fft3_pad(k).reshape(-1, order="F")
-    return ref.spmv(G) / math.sqrt(ref.nnz)
-
-
-def _oracle_adjoint_per_coil(ref, y):
-    import math
-    K = ref.K
-    nc = y.shape[1]
-    G = ref.spmv_t(np.asarray(y, dtype=np.complex128))
-    out = np.empty(tuple(ref.N) + (nc,), dtype=np.complex128)
-    for c in range(nc):
-        g = G[:, c].reshape(K[0], K[1], K[2], 1, order="F")
-        out[..., c] = (ref.ifft3_crop(g) * ref.U[..., None])[..., 0] / math.sqrt(ref.nnz)
-    return out
-
-
 @pytest.mark.slow
 def test_benchmark_workload_per_coil_parity(cuda):
     """N=128^3, koosh ball 256 x 32768, J=6, 8 coils (phantom x coil maps):
@@ -113,7 +89,7 @@ def test_benchmark_workload_per_coil_parity(cuda):
     ref = NufftRef(om, N, J=6, u=2, matrix=False, density_iters=0, workers=os.cpu_count())
     assert obj.nnz == ref.nnz
     k = k_from_dev(obj.fNUFT(img_to_dev(torch, im)))
-    kr = _oracle_forward_per_coil(ref, im)
+    kr = forward_per_coil(ref, im)
     fwd = [rel(k[:, c], kr[:, c]) for c in range(nc)]
     # adjoint of the forward data plus complex noise at 30 dB SNR
     rng = np.random.default_rng(0)
@@ -121,7 +97,7 @@ def test_benchmark_workload_per_coil_parity(cuda):
     y = kr + sig * (rng.standard_normal(kr.shape) + 1j * rng.standard_normal(kr.shape)) / np.sqrt(2)
     del kr
     a = img_from_dev(obj.aNUFT(k_to_dev(torch, y)))
-    ar = _oracle_adjoint_per_coil(ref, y)
+    ar = adjoint_per_coil(ref, y)
     adj = [rel(a[..., c], ar[..., c]) for c in range(nc)]
     print("per-coil rel L2 fwd", ["%.2e" % e for e in fwd], "adj", ["%.2e" % e for e in adj])
     assert max(fwd) < TOL_OP, fwd

@@ -2,7 +2,9 @@
 strict warnings against include/nufft3d.h and a declaration-only mex.h (no
 MATLAB here, so it is type-checked, not linked or run), and the class folder
 exposes the reference's method files."""
+import glob
 import os
+import re
 import shutil
 import subprocess
 
@@ -22,14 +24,70 @@ def test_gateway_type_checks():
     assert r.returncode == 0, r.stderr
 
 
+def _signature(path, name):
+    """Parameter names of `function ... = name(...)` in a MATLAB file."""
+    src = open(path).read()
+    m = re.search(r"^\s*function\s+(?:\[?[\w\s,]*\]?\s*=\s*)?%s\s*\(([^)]*)\)" % name, src, re.M)
+    assert m, (path, name)
+    return [a.strip() for a in m.group(1).split(",") if a.strip()]
+
+
+# The reference class's public methods and argument lists
+# (@nufft_3d/iNUFT.m:2, discrep.m:2, fNUFT.m:2, aNUFT.m:2).
+REFERENCE_SIGNATURES = {
+    "iNUFT": ["obj", "raw", "maxit", "damp", "W", "constraint", "lambda"],
+    "discrep": ["obj", "data", "stddev"],
+    "fNUFT": ["obj", "x"],
+    "aNUFT": ["obj", "k"],
+}
+
+
 def test_class_folder_has_reference_methods():
     cls = os.path.join(MATLAB, "@nufft_3d")
-    for f in ("nufft_3d.m", "fNUFT.m", "aNUFT.m", "iNUFT.m"):
+    for f in ("nufft_3d.m", "fNUFT.m", "aNUFT.m", "iNUFT.m", "discrep.m", "mtimes.m", "ctranspose.m"):
         assert os.path.exists(os.path.join(cls, f)), f
     src = open(os.path.join(cls, "nufft_3d.m")).read()
     for prop in ("J(1,1)", "u(1,1)", "N(1,3)", "alpha(1,1)", "radial(1,1)", "K(1,3)", "nnz(1,1)"):
         assert prop in src, prop
-    # every gateway command the class uses is implemented by the gateway
+
+
+def test_method_argument_order_matches_reference():
+    """The reference's arguments come first, in its order; the class may add
+    trailing optional ones (iNUFT's solver and tol)."""
+    cls = os.path.join(MATLAB, "@nufft_3d")
+    for name, ref_args in REFERENCE_SIGNATURES.items():
+        args = _signature(os.path.join(cls, name + ".m"), name)
+        assert args[:len(ref_args)] == ref_args, (name, args)
+    ref_dir = "/root/reference/@nufft_3d"  # cross-check against the reference itself where it is mounted
+    if os.path.isdir(ref_dir):
+        for name, ref_args in REFERENCE_SIGNATURES.items():
+            assert _signature(os.path.join(ref_dir, name + ".m"), name) == ref_args, name
+
+
+def test_gateway_implements_every_command_the_class_uses():
     gw = open(os.path.join(MATLAB, "nufft3d_mex.c")).read()
-    for cmd in ("create", "info", "deap", "getd", "destroy", "forward", "adjoint", "inverse"):
-        assert '"%s"' % cmd in gw, cmd
+    used = set()
+    for f in glob.glob(os.path.join(MATLAB, "@nufft_3d", "*.m")):
+        used |= set(re.findall(r"nufft3d_mex\('(\w+)'", open(f).read()))
+    assert {"create", "info", "deap", "getd", "destroy", "forward", "adjoint", "inverse", "inverse_x0",
+            "inverse_phase"} <= used
+    for cmd in used:
+        assert 'strcmp(cmd, "%s")' % cmd in gw, cmd
+
+
+def test_demo_call_sequence_maps_onto_the_class():
+    """test_nufft3d.m:55-74 of the reference: constructor with 'gpu', fNUFT,
+    discrep, iNUFT with 1, 3 and 6 arguments ('phase-constraint'); the
+    experimental compressed-sensing call is refused with an error."""
+    cls = os.path.join(MATLAB, "@nufft_3d")
+    calls = [("fNUFT", 1), ("discrep", 2), ("iNUFT", 2), ("iNUFT", 3), ("iNUFT", 6)]
+    for name, nargs in calls:
+        assert len(_signature(os.path.join(cls, name + ".m"), name)) - 1 >= nargs, name
+    src = open(os.path.join(cls, "iNUFT.m")).read()
+    phase = src[src.index("case 'phase-constraint'"):]
+    assert "phase = true" in phase[:80]
+    assert "nufft3d_mex('inverse_phase'" in src
+    cs = src[src.index("case {'compressed-sensing'"):]
+    assert "error(" in cs[:200]
+    ctor = open(os.path.join(cls, "nufft_3d.m")).read()
+    assert "'gpu'" in ctor

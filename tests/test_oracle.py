@@ -101,7 +101,7 @@ def test_cartesian_full_grid_is_scaled_dft_and_density_one():
 
 
 def test_deap_matches_analytic_lewitt():
-    # the analytic branch kept disabled in deap.m:73-128 (radial, not centered)
+    # the analytic branch kept disabled in deap.m:38-95 (radial, not centered)
     rng = np.random.default_rng(0)
     om = rng.uniform(-8, 7, size=(3, 100))
     ref = NufftRef(om, 16, J=6, u=2, density_iters=0)
@@ -120,7 +120,7 @@ def test_deap_matches_analytic_lewitt():
 
 
 def test_diag_qq_close_to_one():
-    # density.m:182-207 diagnostics: diag(Q'Q) ~ 1 and diag(Q'DQ) ~ 1
+    # density.m:44-82 diagnostics: diag(Q'Q) ~ 1 and diag(Q'DQ) ~ 1
     om = synth.koosh_ball(16, 16, 400)
     ref = NufftRef(om, 16, J=6, u=2, density_iters=20)
     N = 16
