@@ -91,6 +91,9 @@ typedef struct nufft3d_info {
     double taps_per_sample; /* mean nonzeros per row of H */
     int64_t device_bytes;   /* device memory held by the plan (tables + scratch) */
     int64_t tap_table_bytes; /* part of device_bytes held by the stored H (0 = none) */
+    int kernel_polynomial;   /* 1: the device evaluates kernel.m's weights as a
+                                polynomial fitted at plan time (max error < 4e-6);
+                                0: with the Numerical Recipes branches of kernel.m */
 } nufft3d_info;
 
 /* Fills *opts with the reference defaults: J=4, u=2, alpha=0 (Beatty),
@@ -114,6 +117,34 @@ int nufft3d_plan_destroy(nufft3d_plan *plan);
  * of one resident trajectory.  nufft3d_density on any handle changes the
  * shared d. */
 int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **plan);
+
+/* Caps the persistent interpolation kernels (gather and spread: one block
+ * per multiprocessor) of this handle at `sms` multiprocessors; 0 = all.  The
+ * others stay free for kernels on other streams -- e.g. the host-link-bound
+ * stages of another handle's host-pointer call, so that two threads calling
+ * nufft3d_forward_host / _adjoint_host on two handles overlap one call's
+ * transfers with the other's compute.  No counterpart in the reference. */
+int nufft3d_plan_set_sms(nufft3d_plan *plan, int sms);
+
+/* Result of nufft3d_plan_tune. */
+typedef struct nufft3d_tune_result {
+    int samples_per_block;  /* chosen largest tile piece (samples) */
+    int coils_per_pass;     /* chosen coils per interpolation pass */
+    double ms_best;         /* fNUFT+aNUFT of nc coils with the choice (ms) */
+    double ms_default;      /* the same with the plan's settings before tuning (0 if cached) */
+    int candidates;         /* settings timed (0 if the choice came from the cache) */
+    int from_cache;         /* 1: taken from an earlier search of the same shape */
+} nufft3d_tune_result;
+
+/* Autotuner: times fNUFT + aNUFT of nc coils (synthetic data) on this plan
+ * for tile pieces of 1024, 2048 or 4096 samples and 2 / 4 / 8 coils per
+ * interpolation pass, keeps the fastest and caches it for the process under
+ * the plan's shape, coil count and sample-density class (later plans of the
+ * same class take it without timing unless force = 1).  The tile shape is
+ * fixed by the kernels and not searched.  Replaces this handle's piece table
+ * (tune before nufft3d_batch_create or nufft3d_plan_share, which copy it).
+ * No counterpart in the reference (sparse H has no blocking to tune). */
+int nufft3d_plan_tune(nufft3d_plan *plan, int nc, int force, nufft3d_tune_result *result);
 
 /* Device bytes a handle allocates for work buffers at nc coils (FFT and
  * interpolation scratch; plus the iNUFT solver vectors if with_solver). */
@@ -248,6 +279,14 @@ int nufft3d_profile_read(nufft3d_plan *plan, char *buf, int cap);
  * nufft3d_density check it themselves.  No counterpart in the reference,
  * whose MATLAB operators are synchronous. */
 int nufft3d_check_status(nufft3d_plan *plan, void *stream);
+
+/* The plan's Kaiser-Bessel weights as the device kernels evaluate them
+ * (kernel.m:2-34): w_dev[i] = kernel(d2_dev[i]) for squared distances in grid
+ * units, 0 <= d2 <= (J/2)^2 (larger d2 gives the value at (J/2)^2, whose
+ * taps the interpolation never keeps).  For checking the single-precision
+ * kernel against the reference's FP64 kernel.m; no counterpart in the
+ * reference. */
+int nufft3d_kernel_eval(const nufft3d_plan *plan, const float *d2_dev, float *w_dev, int64_t n, void *stream);
 
 /* Message of the last failed call on this thread ("" if none). */
 const char *nufft3d_last_error(void);

@@ -48,7 +48,14 @@ class Info(ctypes.Structure):
                 ("nnz", ctypes.c_int64), ("J", ctypes.c_double), ("u", ctypes.c_double),
                 ("alpha", ctypes.c_double), ("radial", ctypes.c_int), ("tile", ctypes.c_int * 3),
                 ("n_blocks", ctypes.c_int64), ("taps_per_sample", ctypes.c_double),
-                ("device_bytes", ctypes.c_int64), ("tap_table_bytes", ctypes.c_int64)]
+                ("device_bytes", ctypes.c_int64), ("tap_table_bytes", ctypes.c_int64),
+                ("kernel_polynomial", ctypes.c_int)]
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("samples_per_block", ctypes.c_int), ("coils_per_pass", ctypes.c_int),
+                ("ms_best", ctypes.c_double), ("ms_default", ctypes.c_double), ("candidates", ctypes.c_int),
+                ("from_cache", ctypes.c_int)]
 
 
 # name -> (restype, argtypes); the exported surface of include/nufft3d.h
@@ -59,6 +66,8 @@ SIGNATURES = {
                                            ctypes.POINTER(ctypes.c_void_p)]),
     "nufft3d_plan_destroy": (ctypes.c_int, [_P]),
     "nufft3d_plan_share": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_void_p)]),
+    "nufft3d_plan_set_sms": (ctypes.c_int, [_P, ctypes.c_int]),
+    "nufft3d_plan_tune": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(TuneResult)]),
     "nufft3d_plan_footprint": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
     "nufft3d_plan_info": (ctypes.c_int, [_P, ctypes.POINTER(Info)]),
     "nufft3d_get_deap": (ctypes.c_int, [_P, _P]),
@@ -89,6 +98,7 @@ SIGNATURES = {
     "nufft3d_batch_adjoint": (ctypes.c_int, [_P, _P, _P, _P]),
     "nufft3d_batch_inverse": (ctypes.c_int, [_P, _P, _P, ctypes.c_int, ctypes.c_double, ctypes.c_double, _P, _P]),
     "nufft3d_check_status": (ctypes.c_int, [_P, _P]),
+    "nufft3d_kernel_eval": (ctypes.c_int, [_P, _P, _P, ctypes.c_int64, _P]),
     "nufft3d_profile": (ctypes.c_int, [_P, ctypes.c_int]),
     "nufft3d_profile_read": (ctypes.c_int, [_P, ctypes.c_char_p, ctypes.c_int]),
     "nufft3d_last_error": (ctypes.c_char_p, []),

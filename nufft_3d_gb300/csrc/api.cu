@@ -462,6 +462,26 @@ extern "C" int nufft3d_density(nufft3d_plan *p, int maxit)
     return NUFFT3D_SUCCESS;
 }
 
+namespace nufft3d {
+__global__ void k_kernel_eval(const float *__restrict__ d2, float *__restrict__ w, int64_t n, KBParams kb)
+{
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) w[i] = kb_weight(fminf(d2[i], kb.half2), kb);
+}
+} // namespace nufft3d
+
+extern "C" int nufft3d_kernel_eval(const nufft3d_plan *p, const float *d2, float *w, int64_t n, void *stream)
+{
+    clear_error();
+    if (!p) return fail(NUFFT3D_ERR_ARG, "plan is NULL");
+    if (n < 0 || (n > 0 && (!d2 || !w))) return fail(NUFFT3D_ERR_ARG, "NULL data pointer or negative count");
+    if (n == 0) return NUFFT3D_SUCCESS;
+    DevGuard g(p->device);
+    k_kernel_eval<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(d2, w, n, p->kb);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
 extern "C" int nufft3d_check_status(nufft3d_plan *p, void *stream)
 {
     clear_error();

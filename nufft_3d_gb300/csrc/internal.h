@@ -102,9 +102,13 @@ __device__ __forceinline__ float kb_weight(float dist2, const KBParams &p)
         return s * p.inv_i0a;
     }
     // large branch: t >= 3.75^2/alpha^2 > 0, so the rsqrt forms are exact enough
-    const float ax = p.alpha * (t * rsqrtf(t));  // alpha*sqrt(t)
+    const float st = t * rsqrtf(t);              // sqrt(t)
+    const float ax = p.alpha * st;               // alpha*sqrt(t)
     const float ra = rsqrtf(ax);                 // ax^(-1/2)
     const float z = 3.75f * (ra * ra);           // 3.75/ax
+    // ax - alpha = -alpha (1 - t) / (1 + sqrt(t)) with 1 - t = dist2/(J/2)^2
+    // taken from the distance itself: no cancellation between ax and alpha
+    const float em = -p.alpha * (dist2 * p.inv_half2) / (1.0f + st);
     float s = fmaf(z, 0.392377e-2f, -0.1647633e-1f);
     s = fmaf(z, s, 0.2635537e-1f);
     s = fmaf(z, s, -0.2057706e-1f);
@@ -113,7 +117,7 @@ __device__ __forceinline__ float kb_weight(float dist2, const KBParams &p)
     s = fmaf(z, s, 0.225319e-2f);
     s = fmaf(z, s, 0.1328592e-1f);
     s = fmaf(z, s, 0.39894228f);
-    return exp_neg(ax - p.alpha) * ra * s * p.exp_over_i0a;
+    return exp_neg(em) * ra * s * p.exp_over_i0a;
 }
 
 // ------------------------------------------------------------ geometry
@@ -305,13 +309,18 @@ struct nufft3d_plan {
     int32_t *perm = nullptr;    // sorted -> original
     int32_t *inv = nullptr;     // original -> sorted, -1 out of bounds
     int4 *blocks = nullptr;     // (tile, start, count, float bits of max summed weight)
+    int4 *own_blocks = nullptr; // a piece table of this handle alone (after nufft3d_plan_tune), else null
     int *cand = nullptr;        // candidate tap offsets (reflected octant), packed
     int n_cand = 0;             // total entries of the 8 sub-cube lists
     nufft3d::Cand cand_desc{};         // device list + per-sub-cube starts and lengths
     int64_t n_blocks = 0;
+    std::vector<int32_t> tile_counts;  // in-bounds samples per tile (host copy; pieces are rebuilt from it)
+    int piece_samples = 0;      // largest piece (samples) of the current piece table
     int coils_per_pass = 8;
+    int max_coils_per_pass = 8; // the largest coil width the plan's shared memory allows
     int use_tma = 1;            // bulk tensor copies for interior gather tiles
     int sm_count = 148;         // multiprocessors of the plan's device
+    int interp_sms = 0;         // SMs the persistent interpolation kernels may use (0 = all)
     int *work = nullptr;        // [16]: work counters of the persistent interpolation kernels and the
                                 // plan's status flags (slots kWork*)
     int wait_polls = nufft3d::kDefaultWaitPolls;  // polls of each bounded wait in the gather
@@ -339,6 +348,15 @@ struct nufft3d_plan {
 };
 
 namespace nufft3d {
+
+// Default largest tile piece (samples): larger pieces measured slightly faster
+// at 128^3 (fewer halo flushes); nufft3d_plan_tune searches around it.
+constexpr int kDefaultPieceSamples = 4096;
+// Tile pieces of at most S samples per tile (split evenly), largest first.
+std::vector<int4> make_pieces(const std::vector<int32_t> &counts, int S);
+// Replaces the plan's piece table with pieces of at most S samples and
+// recomputes their summed-weight bounds (synchronises the plan's stream).
+int rebuild_pieces(nufft3d_plan *p, int S);
 
 // Launchers (stream-ordered, no synchronisation).
 int ensure_scratch(nufft3d_plan *p, int nc);

@@ -1489,6 +1489,8 @@ int plan_check_status(nufft3d_plan *p, cudaStream_t s)
 
 InterpStatus plan_status(const nufft3d_plan *p) { return InterpStatus{p->work + kWorkStatus, p->wait_polls}; }
 
+int interp_grid_sms(const nufft3d_plan *p);
+
 template <int CB, bool RADIAL, int R>
 static int gather_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, int c0, float scale,
                     const float *ws, cudaStream_t s)
@@ -1499,7 +1501,7 @@ static int gather_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, int c0
     std::memset(&m, 0, sizeof(m));
     const int use_tma = p->use_tma && gather_tensor_map<CB>(p, G, nc, &m) ? 1 : 0;
     NUFFT_CUDA_TRY(cudaMemsetAsync(p->work, 0, sizeof(int), s));
-    const int64_t grid = std::min<int64_t>(p->n_blocks, p->sm_count);
+    const int64_t grid = std::min<int64_t>(p->n_blocks, interp_grid_sms(p));
     k_gather<CB, RADIAL, R><<<(unsigned)grid, kInterpThreads, smem, s>>>(
         G, ks, nc, c0, p->samples, p->blocks, (int)p->n_blocks, p->work, p->geom, p->kb, scale, ws, cand_of(p), m,
         use_tma, plan_status(p));
@@ -1512,11 +1514,16 @@ static int spread_t(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, int c0
 {
     const size_t smem = (size_t)IPlane<R>::PS * CB * 2 * sizeof(int) + cand_pairs_bytes(p->cand_desc);
     NUFFT_CUDA_TRY(cudaMemsetAsync(p->work + 1, 0, sizeof(int), s));
-    const int64_t grid = std::min<int64_t>(p->n_blocks, p->sm_count);
+    const int64_t grid = std::min<int64_t>(p->n_blocks, interp_grid_sms(p));
     k_spread<CB, RADIAL, R><<<(unsigned)grid, kInterpThreads, smem, s>>>(
         ks, G, nc, c0, p->samples, p->blocks, (int)p->n_blocks, p->work + 1, p->geom, p->kb, cand_of(p));
     NUFFT_CUDA_TRY(cudaGetLastError());
     return NUFFT3D_SUCCESS;
+}
+
+int interp_grid_sms(const nufft3d_plan *p)
+{
+    return p->interp_sms > 0 && p->interp_sms < p->sm_count ? p->interp_sms : p->sm_count;
 }
 
 bool tap_table_applies(const nufft3d_plan *p) { return p->coils_per_pass == 8 && p->geom.R <= 3; }
@@ -1530,7 +1537,7 @@ static int gather_tab_t(nufft3d_plan *p, const float2 *G, float2 *ks, int nc, in
     std::memset(&m, 0, sizeof(m));
     const int use_tma = p->use_tma && gather_tensor_map<8>(p, G, nc, &m) ? 1 : 0;
     NUFFT_CUDA_TRY(cudaMemsetAsync(p->work, 0, sizeof(int), s));
-    const int64_t grid = std::min<int64_t>(p->n_blocks, p->sm_count);
+    const int64_t grid = std::min<int64_t>(p->n_blocks, interp_grid_sms(p));
     k_gather_tab<R><<<(unsigned)grid, kInterpThreads, smem, s>>>(G, ks, nc, c0, p->blocks, (int)p->n_blocks,
                                                                  p->work, p->geom, scale, ws, p->tap_rows,
                                                                  p->tap_ent, m, use_tma, plan_status(p));

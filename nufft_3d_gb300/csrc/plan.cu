@@ -450,6 +450,7 @@ static void free_plan_memory(nufft3d_plan *p)
     }
     F(p->wbuf);
     F(p->work);
+    F(p->own_blocks);
     F(p->scratch.B1);
     F(p->scratch.B2);
     if (p->scratch.G != p->scratch.B2) F(p->scratch.G); // 2D: G aliases B2
@@ -553,6 +554,26 @@ static int build_tap_table(nufft3d_plan *p, int mode, std::vector<void *> &tmp, 
     return NUFFT3D_SUCCESS;
 }
 
+std::vector<int4> make_pieces(const std::vector<int32_t> &counts, int S)
+{
+    std::vector<int4> blocks;
+    int64_t off = 0;
+    for (size_t t = 0; t < counts.size(); ++t) {
+        const int64_t c = counts[t];
+        if (c > 0) {
+            const int64_t nb = (c + S - 1) / S;
+            for (int64_t b = 0; b < nb; ++b) {
+                const int64_t b0 = c * b / nb, b1 = c * (b + 1) / nb;
+                blocks.push_back(make_int4((int)t, (int)(off + b0), (int)(b1 - b0), 0));
+            }
+        }
+        off += c;
+    }
+    // largest pieces first: the heavy centre of radial k-space starts early
+    std::stable_sort(blocks.begin(), blocks.end(), [](const int4 &a, const int4 &b) { return a.z > b.z; });
+    return blocks;
+}
+
 static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts &o)
 {
     const int64_t M = p->M;
@@ -626,27 +647,16 @@ static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts
     p->nnz = nnz;
 
     // tile pieces of at most S samples, split evenly
-    const int S = o.max_samples_per_block > 0 ? o.max_samples_per_block : 4096;  // larger pieces measured slightly faster (fewer halo flushes)
-    std::vector<int4> blocks;
-    int64_t off = 0;
-    for (uint32_t t = 0; t < ntiles; ++t) {
-        const int64_t c = hc[t];
-        if (c > 0) {
-            const int64_t nb = (c + S - 1) / S;
-            for (int64_t b = 0; b < nb; ++b) {
-                const int64_t b0 = c * b / nb, b1 = c * (b + 1) / nb;
-                blocks.push_back(make_int4((int)t, (int)(off + b0), (int)(b1 - b0), 0));
-            }
-        }
-        off += c;
+    p->tile_counts = std::move(hc);
+    p->piece_samples = o.max_samples_per_block > 0 ? o.max_samples_per_block : kDefaultPieceSamples;
+    {
+        const std::vector<int4> blocks = make_pieces(p->tile_counts, p->piece_samples);
+        p->n_blocks = (int64_t)blocks.size();
+        NUFFT_TRY(dmalloc(&p->blocks, blocks.size(), &p->table_bytes));
+        if (!blocks.empty())
+            NUFFT_CUDA_TRY(cudaMemcpyAsync(p->blocks, blocks.data(), sizeof(int4) * blocks.size(),
+                                           cudaMemcpyHostToDevice, s));
     }
-    // largest pieces first: the heavy centre of radial k-space starts early
-    std::stable_sort(blocks.begin(), blocks.end(), [](const int4 &a, const int4 &b) { return a.z > b.z; });
-    p->n_blocks = (int64_t)blocks.size();
-    NUFFT_TRY(dmalloc(&p->blocks, blocks.size(), &p->table_bytes));
-    if (!blocks.empty())
-        NUFFT_CUDA_TRY(cudaMemcpyAsync(p->blocks, blocks.data(), sizeof(int4) * blocks.size(),
-                                       cudaMemcpyHostToDevice, s));
 
     NUFFT_TRY(dmalloc(&p->samples, (size_t)nnz, &p->table_bytes));
     NUFFT_TRY(dmalloc(&p->inv, (size_t)M, &p->table_bytes));
@@ -868,6 +878,7 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
         return fail(NUFFT3D_ERR_UNSUPPORTED, "interpolation tile too large for shared memory");
     }
     p->coils_per_pass = cb;
+    p->max_coils_per_pass = cb;
     if (cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
         delete p;
         return fail(NUFFT3D_ERR_CUDA, "cudaStreamCreate failed");
@@ -920,10 +931,14 @@ extern "C" int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **out)
     p->inv = src->inv;
     p->blocks = src->blocks;
     p->n_blocks = src->n_blocks;
+    p->tile_counts = src->tile_counts;
+    p->piece_samples = src->piece_samples;
+    p->max_coils_per_pass = src->max_coils_per_pass;
     p->cand = src->cand;
     p->n_cand = src->n_cand;
     p->cand_desc = src->cand_desc;
     p->sm_count = src->sm_count;
+    p->interp_sms = src->interp_sms;
     p->coils_per_pass = src->coils_per_pass;
     p->taps = src->taps;
     p->U = src->U;
@@ -952,7 +967,58 @@ extern "C" int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **out)
         delete p;
         return fail(NUFFT3D_ERR_NOMEM, msg);
     }
+    if (src->own_blocks) {
+        // a tuned source: this handle gets its own copy of the piece table
+        if (dmalloc(&p->own_blocks, (size_t)std::max<int64_t>(p->n_blocks, 1), nullptr) != NUFFT3D_SUCCESS ||
+            cudaMemcpy(p->own_blocks, src->own_blocks, sizeof(int4) * p->n_blocks, cudaMemcpyDeviceToDevice) !=
+                cudaSuccess) {
+            std::string msg = nufft3d_last_error();
+            free_plan_memory(p);
+            p->tables.reset();
+            delete p;
+            return fail(NUFFT3D_ERR_NOMEM, msg.empty() ? std::string("cannot copy the piece table") : msg);
+        }
+        p->blocks = p->own_blocks;
+    }
     *out = p;
+    return NUFFT3D_SUCCESS;
+}
+
+int nufft3d::rebuild_pieces(nufft3d_plan *p, int S)
+{
+    if (S < 32) return fail(NUFFT3D_ERR_ARG, "pieces must hold at least 32 samples");
+    const std::vector<int4> blocks = make_pieces(p->tile_counts, S);
+    int4 *nb = nullptr;
+    NUFFT_TRY(dmalloc(&nb, std::max<size_t>(blocks.size(), 1), nullptr));
+    cudaStream_t s = p->own_stream;
+    cudaError_t e = blocks.empty() ? cudaSuccess
+                                   : cudaMemcpyAsync(nb, blocks.data(), sizeof(int4) * blocks.size(),
+                                                     cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        NUFFT_DEVICE_LOCK;
+        cudaFree(nb);
+        return fail(NUFFT3D_ERR_CUDA, std::string("piece table: ") + cudaGetErrorString(e));
+    }
+    {
+        NUFFT_DEVICE_LOCK;
+        if (p->own_blocks) cudaFree(p->own_blocks);
+    }
+    p->own_blocks = nb;
+    p->blocks = nb;
+    p->n_blocks = (int64_t)blocks.size();
+    p->piece_samples = S;
+    NUFFT_TRY(launch_weight_sum(p, s));
+    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    return NUFFT3D_SUCCESS;
+}
+
+extern "C" int nufft3d_plan_set_sms(nufft3d_plan *p, int sms)
+{
+    clear_error();
+    if (!p) return fail(NUFFT3D_ERR_ARG, "plan is NULL");
+    if (sms < 0) return fail(NUFFT3D_ERR_ARG, "sms must be nonnegative");
+    p->interp_sms = sms;
     return NUFFT3D_SUCCESS;
 }
 
@@ -1003,6 +1069,7 @@ extern "C" int nufft3d_plan_info(const nufft3d_plan *p, nufft3d_info *info)
     info->taps_per_sample = p->taps;
     info->device_bytes = p->table_bytes + (int64_t)p->scratch.bytes;
     info->tap_table_bytes = p->tap_bytes;
+    info->kernel_polynomial = p->kb.poly;
     return NUFFT3D_SUCCESS;
 }
 

@@ -151,6 +151,17 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
         t._adjoint = False
         return t
 
+    def tune(self, nc, force=False):
+        """Autotuner (nufft3d_plan_tune): times fNUFT+aNUFT of nc coils over
+        piece sizes and coils per pass, keeps the fastest (cached per shape
+        class).  Returns the choice and timings as a dict."""
+        r = _lib.TuneResult()
+        _lib.check(self._L.nufft3d_plan_tune(self.plan, int(nc), int(bool(force)), ctypes.byref(r)))
+        self.n_blocks = int(self.info()["n_blocks"])
+        return {"samples_per_block": r.samples_per_block, "coils_per_pass": r.coils_per_pass,
+                "ms_best": r.ms_best, "ms_default": r.ms_default, "candidates": r.candidates,
+                "from_cache": bool(r.from_cache)}
+
     def footprint(self, nc, with_solver=True):
         b = ctypes.c_int64()
         _lib.check(self._L.nufft3d_plan_footprint(self.plan, int(nc), int(bool(with_solver)), ctypes.byref(b)))

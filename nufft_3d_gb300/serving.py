@@ -52,6 +52,7 @@ class Request:
     # filled by the server
     t_start: float = 0.0
     t_done: float = 0.0
+    plan_s: float = 0.0            # time spent building this request's plan (0 if resident)
     result: np.ndarray = None
 
     def __post_init__(self):
@@ -266,6 +267,7 @@ class ReconServer:
             t0 = time.perf_counter()
             try:
                 h = self._acquire_handle(slot, req0, entry, new_plan)
+                t_plan = time.perf_counter() - t0 if new_plan else 0.0
                 raws = [r.raw.reshape(r.raw.shape[0], -1) for r, _ in batch]
                 raw = np.concatenate(raws, axis=1) if len(raws) > 1 else raws[0]
                 im = h.iNUFT(raw, req0.maxit, req0.damp, solver=req0.solver, tol=req0.tol)
@@ -276,6 +278,7 @@ class ReconServer:
                     c += r.nc
                     r.t_start = t0
                     r.t_done = t1
+                    r.plan_s = t_plan
                     fut.set_result(r)
             except Exception as e:  # report to every waiting request
                 if new_plan:
@@ -355,6 +358,7 @@ def run_plain(requests, device=0):
             time.sleep(delay)
         r.t_start = time.perf_counter() - start
         obj = nufft_3d(r.om, r.N, device=device, **r.opts)
+        r.plan_s = time.perf_counter() - start - r.t_start
         r.result = obj.iNUFT(r.raw.reshape(r.raw.shape[0], -1), r.maxit, r.damp, solver=r.solver, tol=r.tol)
         obj.close()
         r.t_done = time.perf_counter() - start
@@ -363,7 +367,9 @@ def run_plain(requests, device=0):
 
 def summarize(requests, wall):
     lat = np.array([r.latency for r in requests]) * 1e3
+    built = [r.plan_s for r in requests if r.plan_s > 0]
     return {"requests": len(requests), "wall_s": round(wall, 3),
             "volumes_per_s": round(len(requests) / wall, 3),
             "p50_ms": round(float(np.percentile(lat, 50)), 2), "p99_ms": round(float(np.percentile(lat, 99)), 2),
-            "mean_ms": round(float(lat.mean()), 2)}
+            "mean_ms": round(float(lat.mean()), 2), "plans_built": len(built),
+            "plan_build_ms_mean": round(1e3 * float(np.mean(built)), 2) if built else 0.0}

@@ -41,7 +41,8 @@ def test_header_struct_fields_match_ctypes():
     """Every field of nufft3d_opts / nufft3d_info in include/nufft3d.h is mirrored, in order."""
     import os, re
     hdr = open(os.path.join(os.path.dirname(__file__), "..", "include", "nufft3d.h")).read()
-    for cname, cls in (("nufft3d_opts", _lib.Opts), ("nufft3d_info", _lib.Info)):
+    for cname, cls in (("nufft3d_opts", _lib.Opts), ("nufft3d_info", _lib.Info),
+                       ("nufft3d_tune_result", _lib.TuneResult)):
         body = re.search(r"typedef struct %s \{(.*?)\} %s;" % (cname, cname), hdr, re.S).group(1)
         body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
         names = []
@@ -126,3 +127,19 @@ def test_solver_entry_points_check_arguments_without_a_device():
 def test_check_status_rejects_null_plan():
     L = _lib.load()
     assert L.nufft3d_check_status(None, None) == _lib.ERR_ARG
+
+
+def test_set_sms_rejects_null_plan():
+    L = _lib.load()
+    assert L.nufft3d_plan_set_sms(None, 4) == _lib.ERR_ARG
+
+
+def test_tune_rejects_bad_arguments():
+    L = _lib.load()
+    r = _lib.TuneResult()
+    assert L.nufft3d_plan_tune(None, 8, 0, ctypes.byref(r)) == _lib.ERR_ARG
+
+
+def test_kernel_eval_checks_arguments():
+    L = _lib.load()
+    assert L.nufft3d_kernel_eval(None, None, None, 4, None) == _lib.ERR_ARG
