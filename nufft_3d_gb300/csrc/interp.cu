@@ -1050,21 +1050,21 @@ __device__ __forceinline__ bool gather_piece_tab(const float2 *__restrict__ G, f
     auto step = [&](int2 &ed, uint32_t ch) {
         const int2 cur = ed;
         ed = ch + 4 < nchk ? ld_tap(st + (size_t)(ch + 4) * 8) : z2;
-        if (cur.x != 0) {
-            // coil pairs in the rotated order rot ^ k (see accumulate)
-            const float w = __int_as_float(cur.x);
-            const float2 ww = make_float2(w, w);
-            const char *pb = reinterpret_cast<const char *>(tile) + (size_t)cur.y * (CB * 8);
+        // coil pairs in the rotated order rot ^ k (see accumulate); padding
+        // entries (weight 0, tile offset 0) add nothing and need no branch
+        const float w = __int_as_float(cur.x);
+        const float2 ww = make_float2(w, w);
+        const char *pb = reinterpret_cast<const char *>(tile) + (size_t)cur.y * (CB * 8);
 #pragma unroll
-            for (int k = 0; k < CB / 2; ++k) {
-                const float4 v = *reinterpret_cast<const float4 *>(pb + (rot16 ^ (k << 4)));
-                acc[2 * k] = __ffma2_rn(ww, make_float2(v.x, v.y), acc[2 * k]);
-                acc[2 * k + 1] = __ffma2_rn(ww, make_float2(v.z, v.w), acc[2 * k + 1]);
-            }
+        for (int k = 0; k < CB / 2; ++k) {
+            const float4 v = *reinterpret_cast<const float4 *>(pb + (rot16 ^ (k << 4)));
+            acc[2 * k] = __ffma2_rn(ww, make_float2(v.x, v.y), acc[2 * k]);
+            acc[2 * k + 1] = __ffma2_rn(ww, make_float2(v.z, v.w), acc[2 * k + 1]);
         }
         if (ch + 1 == send) {
-            finish();
-            while (s < s_hi && send == ch + 1) finish();
+            do {
+                finish();
+            } while (s < s_hi && send == ch + 1);  // and the samples without taps after it
         }
     };
     for (uint32_t ch = 0; ch < nchk; ch += 4) {
