@@ -469,6 +469,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the plan-time autotuner")
     ap.add_argument("--tap-table", dest="tap_table", type=int, default=-1, choices=[-1, 0, 1],
                     help="stored H: -1 auto (library default), 0 evaluate taps on the fly, 1 always")
+    ap.add_argument("--spread-table", dest="spread_table", type=int, default=-1, choices=[-1, 0, 1],
+                    help="stored H' for the 8-coil spread: -1 auto (library default), 0 on the fly, 1 always")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -482,7 +484,8 @@ def main():
     om, im = build_inputs(args.N, args.n_read, args.n_spokes, args.nc)
     tile = tuple(int(t) for t in args.tile.split(",")) if args.tile else None
     obj = nufft_3d(om, args.N, "J", 6, "u", 2, device=local, tile=tile, coils_per_pass=args.coils_per_pass,
-                   samples_per_block=args.samples_per_block, tap_table=args.tap_table)
+                   samples_per_block=args.samples_per_block, tap_table=args.tap_table,
+                   spread_table=args.spread_table)
     L, plan = obj._L, obj.plan
     nc, M = args.nc, obj.M
     # the plan-time autotuner picks the piece size and coils per pass
@@ -603,6 +606,13 @@ def main():
         g["stored_h_bytes"] = hb
         g["achieved_gbs_with_stored_h"] = round((g["algo_bytes_per_launch"] + hb) /
                                                 (g["ms_per_step"] / 1e3 / max(1, g["launches"] // args.steps)) / 1e9, 1)
+    if "spread" in stages and obj.spread_table_bytes and nc >= 8:
+        # the stored H' read by the 8-coil spread passes, beside its algorithmic bytes
+        hb = obj.spread_table_bytes * (nc // 8)
+        g = stages["spread"]
+        g["stored_h_t_bytes"] = hb
+        g["achieved_gbs_with_stored_h_t"] = round((g["algo_bytes_per_launch"] + hb) /
+                                                  (g["ms_per_step"] / 1e3 / max(1, g["launches"] // args.steps)) / 1e9, 1)
     launches = sum(r["launches"] for r in prof.values())
     ours_fft = {"fwd": sum(stages[n]["ms_per_step"] for n in ("fft_x_fwd", "fft_y_fwd", "fft_z_fwd") if n in stages),
                 "adj": sum(stages[n]["ms_per_step"] for n in ("fft_x_adj", "fft_y_adj", "fft_z_adj") if n in stages)}
@@ -619,7 +629,7 @@ def main():
             "data": "synthetic",
             "config": {"workload": WORKLOAD, "N": args.N, "M": M, "nnz": obj.nnz, "nc": nc,
                        "taps_per_sample": round(obj.taps_per_sample, 2), "tile": list(obj.tile),
-                       "stored_h_bytes": obj.tap_table_bytes,
+                       "stored_h_bytes": obj.tap_table_bytes, "stored_h_t_bytes": obj.spread_table_bytes,
                        "blocks": obj.info()["n_blocks"], "l2": "inputs larger than L2 (grid 1.07 GB), no flush",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "e2e": {"value": round(e2e, 2), "unit": "Msample/s", "h2d_bytes_per_step": h2d,

@@ -66,7 +66,7 @@ typedef struct nufft3d_opts {
     int verbose;       /* print the reference's set-up summary to stdout */
     int tap_table;     /* stored interpolation matrix H (nufft_3d.m:153-212) in
                           tile order, read by the 8-coil gather passes of fNUFT
-                          (H' is applied on the fly): 1 = build it, 0 = evaluate
+                          (see spread_table for H'): 1 = build it, 0 = evaluate
                           the kernel on the fly, -1 = auto (default: build it
                           when it takes at most half of the free device memory) */
     int wait_polls;    /* polls of each bounded wait of the interpolation
@@ -76,6 +76,13 @@ typedef struct nufft3d_opts {
                           copy is then still allowed to land, but its tile is
                           skipped and the timeout reported, which exercises the
                           error path without a fault */
+    int spread_table;  /* stored transpose H' (built from the stored H, so only
+                          with it), read by the 8-coil spread passes of aNUFT
+                          (full passes of an even coil count): per tile piece
+                          of at most 2048 samples, each grid point's row of
+                          (sample, weight); 1 = build it, 0 = evaluate the
+                          kernel on the fly, -1 = auto (default: build it when
+                          it takes at most half of the free device memory) */
 } nufft3d_opts;
 
 /* Read-only properties (nufft_3d.m:26-43). */
@@ -94,11 +101,12 @@ typedef struct nufft3d_info {
     int kernel_polynomial;   /* 1: the device evaluates kernel.m's weights as a
                                 polynomial fitted at plan time (max error < 4e-6);
                                 0: with the Numerical Recipes branches of kernel.m */
+    int64_t spread_table_bytes; /* part of device_bytes held by the stored H' (0 = none) */
 } nufft3d_info;
 
 /* Fills *opts with the reference defaults: J=4, u=2, alpha=0 (Beatty),
  * radial=1, gpu=1, density_iters=20 (nufft_3d.m:27-36, density.m:5),
- * tap_table=-1. */
+ * tap_table=-1, spread_table=-1. */
 int nufft3d_opts_default(nufft3d_opts *opts);
 
 /* obj = nufft_3d(om, N, name, value, ...)  -- nufft_3d.m:54-251.

@@ -40,7 +40,7 @@ class Opts(ctypes.Structure):
                 ("d", ctypes.c_void_p), ("density_iters", ctypes.c_int),
                 ("tile", ctypes.c_int * 3), ("max_coils_per_pass", ctypes.c_int),
                 ("max_samples_per_block", ctypes.c_int), ("verbose", ctypes.c_int),
-                ("tap_table", ctypes.c_int), ("wait_polls", ctypes.c_int)]
+                ("tap_table", ctypes.c_int), ("wait_polls", ctypes.c_int), ("spread_table", ctypes.c_int)]
 
 
 class Info(ctypes.Structure):
@@ -49,7 +49,7 @@ class Info(ctypes.Structure):
                 ("alpha", ctypes.c_double), ("radial", ctypes.c_int), ("tile", ctypes.c_int * 3),
                 ("n_blocks", ctypes.c_int64), ("taps_per_sample", ctypes.c_double),
                 ("device_bytes", ctypes.c_int64), ("tap_table_bytes", ctypes.c_int64),
-                ("kernel_polynomial", ctypes.c_int)]
+                ("kernel_polynomial", ctypes.c_int), ("spread_table_bytes", ctypes.c_int64)]
 
 
 class TuneResult(ctypes.Structure):

@@ -330,6 +330,14 @@ struct nufft3d_plan {
     uint32_t *tap_rows = nullptr;
     int2 *tap_ent = nullptr;
     int64_t tap_bytes = 0;
+    // stored H' for the 8-coil spread (spread_tab.cu): pieces of at most
+    // kSpreadCap samples, (tile, first sample, count, first line); the warps'
+    // first lines (33 per piece); the bundles of 128-byte lines
+    int4 *spread_pieces = nullptr;
+    uint32_t *spread_wstart = nullptr;
+    int2 *spread_ent = nullptr;
+    int64_t n_spread_pieces = 0;
+    int64_t spread_bytes = 0;
     int threads = 256;
     double taps = 0;
     float *U = nullptr;         // deapodization [N1 N2 N3]
@@ -382,6 +390,16 @@ int launch_tap_fill(nufft3d_plan *p, const uint32_t *rows, int2 *taps, cudaStrea
 bool tap_table_applies(const nufft3d_plan *p);
 // spread: G += H' ks (G zeroed by caller)
 int launch_spread(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, cudaStream_t s);
+// Largest spread piece of the stored H' (samples staged in shared memory).
+constexpr int kSpreadCap = 2048;
+// stored H' (spread_tab.cu): plan-time build from the stored H, the 8-coil
+// spread pass that reads it, and whether it serves coils c0..c0+7 of nc
+int build_spread_table(nufft3d_plan *p, int mode, cudaStream_t s);
+int launch_spread_tab(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, int c0, cudaStream_t s);
+bool spread_tab_applies(const nufft3d_plan *p, int nc, int c0);
+int configure_spread_tab_kernels();
+// multiprocessors the persistent interpolation kernels of a handle may use
+int interp_grid_sms(const nufft3d_plan *p);
 // user [M nc] <-> sorted [nnz][nc]
 int launch_permute_out(nufft3d_plan *p, const float2 *ks, float2 *k, int nc, float scale,
                        cudaStream_t s);

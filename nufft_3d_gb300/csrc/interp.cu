@@ -1599,9 +1599,14 @@ static int interp(nufft3d_plan *p, const float2 *in, float2 *out, int nc, float 
         case 2: st = dispatch<GATHER, 2>(p, in, out, nc, c0, scale, ws, s); break;
         case 4: st = dispatch<GATHER, 4>(p, in, out, nc, c0, scale, ws, s); break;
         default:
-            // the stored H serves the gather; the spread applies H' on the fly
-            st = GATHER && p->tap_ent ? gather_tab(p, in, out, nc, c0, scale, ws, s)
-                                      : dispatch<GATHER, 8>(p, in, out, nc, c0, scale, ws, s);
+            // the stored H serves the gather and the stored H' the spread
+            // (full passes of an even coil count), else the kernel is evaluated
+            if (GATHER && p->tap_ent)
+                st = gather_tab(p, in, out, nc, c0, scale, ws, s);
+            else if (!GATHER && spread_tab_applies(p, nc, c0))
+                st = launch_spread_tab(p, in, out, nc, c0, s);
+            else
+                st = dispatch<GATHER, 8>(p, in, out, nc, c0, scale, ws, s);
             break;
         }
         if (st != NUFFT3D_SUCCESS) return st;

@@ -403,6 +403,7 @@ int configure_kernels()
     NUFFT_DEVICE_LOCK; // constant-memory uploads must not overlap a stream capture
     NUFFT_TRY(configure_fft_kernels());
     NUFFT_TRY(configure_interp_kernels());
+    NUFFT_TRY(configure_spread_tab_kernels());
     if (dev < 32) done_mask |= 1 << dev;
     return NUFFT3D_SUCCESS;
 }
@@ -424,7 +425,7 @@ static void adopt_tables(nufft3d_plan *p)
     auto t = std::make_shared<TableOwner>();
     t->device = p->device;
     t->ptrs = {p->samples, p->perm, p->inv, p->blocks, p->cand, p->U, p->d, p->d_orig,
-               p->tw[0], p->tw[1], p->tw[2], p->tap_rows, p->tap_ent};
+               p->tw[0], p->tw[1], p->tw[2], p->tap_rows, p->tap_ent, p->spread_pieces, p->spread_wstart, p->spread_ent};
     p->tables = t;
 }
 
@@ -447,6 +448,9 @@ static void free_plan_memory(nufft3d_plan *p)
         for (int a = 0; a < 3; ++a) F(p->tw[a]);
         F(p->tap_rows);
         F(p->tap_ent);
+        F(p->spread_pieces);
+        F(p->spread_wstart);
+        F(p->spread_ent);
     }
     F(p->wbuf);
     F(p->work);
@@ -699,6 +703,7 @@ static int build_plan(nufft3d_plan *p, const double *om_host, const nufft3d_opts
     }
     NUFFT_TRY(launch_weight_sum(p, s));
     NUFFT_TRY(build_tap_table(p, o.tap_table, tmp.ptrs, s));
+    NUFFT_TRY(build_spread_table(p, o.spread_table, s));
     // deapodization (FP64 on the host, stored FP32 like deap.m:100-101)
     {
         std::vector<double> U = deap_host(p->N, g.K, p->J, p->alpha, g.radial, g.is2d);
@@ -773,6 +778,7 @@ extern "C" int nufft3d_opts_default(nufft3d_opts *o)
     o->density_iters = 20;
     o->tap_table = -1;
     o->wait_polls = kDefaultWaitPolls;
+    o->spread_table = -1;
     return NUFFT3D_SUCCESS;
 }
 
@@ -902,6 +908,8 @@ extern "C" int nufft3d_plan_create(const double *om, int64_t M, const int32_t *N
                     (long long)p->nnz, (long long)M, p->taps, (long long)p->n_blocks);
         if (p->tap_ent)
             std::printf("  stored H: %.1f MB\n", (double)p->tap_bytes / 1e6);
+        if (p->spread_ent)
+            std::printf("  stored H': %.1f MB\n", (double)p->spread_bytes / 1e6);
     }
     *out = p;
     return NUFFT3D_SUCCESS;
@@ -951,6 +959,11 @@ extern "C" int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **out)
     p->tap_rows = src->tap_rows;
     p->tap_ent = src->tap_ent;
     p->tap_bytes = src->tap_bytes;
+    p->spread_pieces = src->spread_pieces;
+    p->spread_wstart = src->spread_wstart;
+    p->spread_ent = src->spread_ent;
+    p->n_spread_pieces = src->n_spread_pieces;
+    p->spread_bytes = src->spread_bytes;
     p->table_bytes = src->table_bytes;
     p->tables = src->tables;
     if (cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -1070,6 +1083,7 @@ extern "C" int nufft3d_plan_info(const nufft3d_plan *p, nufft3d_info *info)
     info->device_bytes = p->table_bytes + (int64_t)p->scratch.bytes;
     info->tap_table_bytes = p->tap_bytes;
     info->kernel_polynomial = p->kb.poly;
+    info->spread_table_bytes = p->spread_bytes;
     return NUFFT3D_SUCCESS;
 }
 

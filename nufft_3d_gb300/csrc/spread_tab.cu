@@ -1,0 +1,468 @@
+// Spread (aNUFT's H' product, spmv_t of nufft_3d.m:274-282) from a stored
+// transpose of H, for 8-coil passes.
+//
+// The reference multiplies by the transpose of its sparse H through cuSPARSE.
+// The on-the-fly spread (interp.cu) scatters each sample's taps into a tile
+// with shared-memory integer reductions, which bounds it by instruction issue
+// and the reduction pipe.  This form turns the product around: the samples of
+// a tile piece are staged in shared memory, and each grid point of the
+// piece's padded tile (tile plus halo) owns a row of (sample, weight) entries
+// -- H' restricted to the piece.  Four lanes (one per coil pair) walk a row,
+// accumulate the grid point's 8 coils in registers with FP32 FMAs, and add
+// the finished point to the grid with one 16-byte vector atomic each
+// (neighbouring pieces' halos overlap).  No shared-memory atomics, no kernel
+// evaluation, and FP32 accumulation throughout.
+//
+// Stored H' layout, per spread piece (at most kSpreadCap samples of one
+// tile, so that their 8 coils fit in shared memory):
+//   * the piece's non-empty rows are sorted by length (longest first, ties
+//     by grid point) and taken 8 at a time into bundles; a bundle is a run of
+//     128-byte lines, one 16-byte unit per row slot (row slot r = lanes
+//     4r..4r+3 of a warp), so a warp walks 8 rows in lockstep and every
+//     branch on the bundle structure is warp-uniform;
+//   * line 0 of a bundle is its header: per row slot int4 (B, y, 0, 0) with
+//     B the bundle's body lines and y = -1 - (grid point index), or 0 for a
+//     slot without a row (the last bundle of a piece);
+//   * each body line holds two entries per row slot, int2 (weight bits,
+//     byte offset of the sample's 64-byte slot in the staged samples: local
+//     index + 2; slots 0 and 1 stay zero and serve as padding);
+//   * inside a row, even-slot and odd-slot samples alternate, starting with
+//     the parity of the row slot, so the two rows a quarter-warp reads in one
+//     instruction touch different halves of the shared-memory banks;
+//     leftovers of the larger parity and padding (weight 0) follow;
+//   * the piece's bundles are split into 32 contiguous runs of about equal
+//     length, one per warp: wstart[33 * piece + w] is warp w's first line.
+// Inside a row the samples keep their sorted order (the fill is
+// deterministic), so the FP32 sums do not depend on scheduling.
+//
+// The table is built from the stored H (same weights, same support test)
+// once per plan: a count pass gives each piece's lines, the host scans them,
+// and a fill pass writes the bundles.
+#include <cub/block/block_radix_sort.cuh>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "internal.h"
+
+namespace nufft3d {
+
+constexpr int kTabBuildThreads = 256;
+constexpr int kTabBuildWarps = kTabBuildThreads / 32;
+constexpr int kTabSortItems = 11;  // 256 x 11 >= 14^3 padded-tile points
+constexpr int kSpreadThreads = 1024;
+constexpr int kSpreadWarps = kSpreadThreads / 32;
+constexpr int kSpreadDepth = 5;    // lines each lane keeps in flight
+constexpr int kMaxBundles = (kTabBuildThreads * kTabSortItems + 7) / 8;
+
+// Origin of the padded tile of tile index tid (may be negative or past the
+// grid edge: the grid wraps around).
+__device__ __forceinline__ void tab_tile_origin(const Geom &g, int tid, int &ox, int &oy, int &oz)
+{
+    const int tx = tid % g.nt[0];
+    const int ty = (tid / g.nt[0]) % g.nt[1];
+    const int tz = tid / (g.nt[0] * g.nt[1]);
+    ox = tx * g.T[0] - g.Ra[0];
+    oy = ty * g.T[1] - g.Ra[1];
+    oz = tz * g.T[2] - g.Ra[2];
+}
+
+__device__ __forceinline__ int tab_wrap(int x, int K)
+{
+    x %= K;
+    return x < 0 ? x + K : x;
+}
+
+using TabSort = cub::BlockRadixSort<uint32_t, kTabBuildThreads, kTabSortItems>;
+
+struct TabBuildSmem {
+    typename TabSort::TempStorage sort;
+    uint32_t ubase[kMaxBundles + 1];  // first line of each bundle (piece-relative); [nb] = total
+    int nrows;
+};
+
+// Plan time, one block per spread piece.  FILL = false: writes the piece's
+// line count to lines_out[b].  FILL = true: writes the piece's bundles from
+// line pieces[b].w on and the warps' first lines to wstart[33 b ..].
+// Dynamic shared memory: per-warp packed counts [warps][P] (even-slot count
+// | odd-slot count << 16), the row totals [P] and each point's row rank [P].
+// Warp w takes a contiguous run of the piece's samples, one sample at a time
+// (a sample's taps are distinct points, so its lanes never update the same
+// counter), which makes each row's entries come out in sample order.
+template <bool FILL>
+__global__ void __launch_bounds__(kTabBuildThreads)
+k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__ rows,
+                   const int2 *__restrict__ taps, Geom g, uint32_t *__restrict__ lines_out,
+                   uint32_t *__restrict__ wstart, int2 *__restrict__ ent)
+{
+    extern __shared__ uint32_t sm[];
+    __shared__ TabBuildSmem ss;
+    const int P = g.P[0] * g.P[1] * g.P[2];
+    uint32_t *hist = sm;
+    uint32_t *tot = sm + kTabBuildWarps * P;
+    uint32_t *rank = tot + P;  // row rank of point p (sorted order), or ~0u
+    const int4 pc = pieces[blockIdx.x];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < kTabBuildWarps * P; i += blockDim.x) hist[i] = 0;
+    __syncthreads();
+    const int s_lo = pc.y + (int)(((long long)pc.z * warp) / kTabBuildWarps);
+    const int s_hi = pc.y + (int)(((long long)pc.z * (warp + 1)) / kTabBuildWarps);
+    uint32_t *h = hist + (size_t)warp * P;
+    for (int s = s_lo; s < s_hi; ++s) {
+        const size_t r0 = (size_t)__ldg(&rows[s]) * 8, r1 = (size_t)__ldg(&rows[s + 1]) * 8;
+        const uint32_t inc = ((s - pc.y) & 1) ? 0x10000u : 1u;
+        for (size_t e = r0 + lane; e < r1; e += 32) {
+            const int2 t = __ldg(&taps[e]);
+            if (t.x != 0) h[t.y] += inc;  // padding entries have weight 0
+        }
+        __syncwarp();
+    }
+    __syncthreads();
+    // per point: exclusive prefix over the warps and the row's total
+    for (int p = tid; p < P; p += blockDim.x) {
+        uint32_t acc = 0;
+        for (int w = 0; w < kTabBuildWarps; ++w) {
+            const uint32_t v = hist[(size_t)w * P + p];
+            hist[(size_t)w * P + p] = acc;
+            acc += v;
+        }
+        tot[p] = acc;
+    }
+    __syncthreads();
+    // rows by length, longest first, ties by point: key (4095 - L) << 12 | p
+    uint32_t key[kTabSortItems];
+#pragma unroll
+    for (int i = 0; i < kTabSortItems; ++i) {
+        const int p = tid * kTabSortItems + i;
+        uint32_t k = 0xFFFFFFFFu;
+        if (p < P) {
+            const uint32_t a = tot[p], L = (a & 0xFFFFu) + (a >> 16);
+            k = ((4095u - L) << 12) | (uint32_t)p;
+        }
+        key[i] = k;
+    }
+    if (tid == 0) ss.nrows = 0;
+    __syncthreads();  // (tot is read above; nrows is counted below)
+    TabSort(ss.sort).Sort(key, 0, 24);
+    // blocked arrangement: thread t holds sorted positions t*items + i; the
+    // rows (points with entries) come first
+#pragma unroll
+    for (int i = 0; i < kTabSortItems; ++i) {
+        const uint32_t k = key[i];
+        if (k == 0xFFFFFFFFu) continue;
+        const bool row = (k >> 12) != 4095u;
+        rank[k & 0xFFFu] = row ? (uint32_t)(tid * kTabSortItems + i) : 0xFFFFFFFFu;
+        if (row) atomicAdd(&ss.nrows, 1);
+    }
+    __syncthreads();
+    const int nr = ss.nrows, nb = (nr + 7) / 8;
+    // bundle lengths: a bundle's first row is its longest
+    for (int p = tid; p < P; p += blockDim.x) {
+        const uint32_t r = rank[p];
+        if (r != 0xFFFFFFFFu && (r & 7u) == 0) {
+            const uint32_t a = tot[p], L = (a & 0xFFFFu) + (a >> 16);
+            ss.ubase[r >> 3] = 1u + (L + 1u) / 2u;  // header + body lines
+        }
+    }
+    __syncthreads();
+    if (tid == 0) {
+        uint32_t a = 0;
+        for (int k = 0; k < nb; ++k) {
+            const uint32_t v = ss.ubase[k];
+            ss.ubase[k] = a;
+            a += v;
+        }
+        ss.ubase[nb] = a;
+    }
+    __syncthreads();
+    const uint32_t nlines = ss.ubase[nb];
+    if (!FILL) {
+        if (tid == 0) lines_out[blockIdx.x] = nlines;
+        return;
+    }
+    const uint32_t base = (uint32_t)pc.w;
+    // warp runs: warp w starts at the first bundle whose first line is at or
+    // past w/32 of the piece's lines
+    if (tid <= kSpreadWarps) {
+        const uint32_t target = (uint32_t)(((unsigned long long)nlines * tid) / kSpreadWarps);
+        int lo = 0, hi = nb;  // first k in [0, nb] with ubase[k] >= target
+        while (lo < hi) {
+            const int mid = (lo + hi) / 2;
+            if (ss.ubase[mid] >= target) hi = mid;
+            else lo = mid + 1;
+        }
+        wstart[(size_t)blockIdx.x * (kSpreadWarps + 1) + tid] = base + ss.ubase[lo];
+    }
+    // entry j of row slot r of the bundle whose first line is l0
+    auto at = [&](uint32_t l0, int r, uint32_t j) -> size_t {
+        return (((size_t)base + l0 + 1u + j / 2u) * 8u + (size_t)r) * 2u + (j & 1u);
+    };
+    // headers and padding
+    int ox, oy, oz;
+    tab_tile_origin(g, pc.x, ox, oy, oz);
+    for (int p = tid; p < P; p += blockDim.x) {
+        const uint32_t rr = rank[p];
+        if (rr == 0xFFFFFFFFu) continue;
+        const int k = (int)(rr >> 3), r = (int)(rr & 7u);
+        const uint32_t l0 = ss.ubase[k], B = ss.ubase[k + 1] - l0 - 1u;
+        const uint32_t a = tot[p], L = (a & 0xFFFFu) + (a >> 16);
+        const int lx = p % g.P[0], ly = (p / g.P[0]) % g.P[1], lz = p / (g.P[0] * g.P[1]);
+        const long long gi = ((long long)tab_wrap(oz + lz, g.K[2]) * g.K[1] + tab_wrap(oy + ly, g.K[1])) * g.K[0] +
+                             tab_wrap(ox + lx, g.K[0]);
+        reinterpret_cast<int4 *>(ent)[((size_t)base + l0) * 8u + r] = make_int4((int)B, (int)(-1 - gi), 0, 0);
+        for (uint32_t j = L; j < 2u * B; ++j) ent[at(l0, r, j)] = make_int2(0, 64 * (int)((j + r) & 1u));
+    }
+    // row slots without a row (last bundle)
+    if (tid < 8 && nb > 0 && nr + tid < nb * 8) {
+        const int r = (nr + tid) & 7, k = nb - 1;
+        const uint32_t l0 = ss.ubase[k], B = ss.ubase[k + 1] - l0 - 1u;
+        reinterpret_cast<int4 *>(ent)[((size_t)base + l0) * 8u + r] = make_int4((int)B, 0, 0, 0);
+        for (uint32_t j = 0; j < 2u * B; ++j) ent[at(l0, r, j)] = make_int2(0, 64 * (int)((j + r) & 1u));
+    }
+    // the entries: row slot r starts with parity r & 1, then alternates while
+    // both parities last; leftovers follow in sample order
+    for (int s = s_lo; s < s_hi; ++s) {
+        const int sl = s - pc.y, par = sl & 1;
+        const uint32_t inc = par ? 0x10000u : 1u;
+        const size_t r0 = (size_t)__ldg(&rows[s]) * 8, r1 = (size_t)__ldg(&rows[s + 1]) * 8;
+        for (size_t e = r0 + lane; e < r1; e += 32) {
+            const int2 t = __ldg(&taps[e]);
+            if (t.x == 0) continue;
+            const int p = t.y;
+            const uint32_t hv = h[p];
+            h[p] = hv + inc;
+            const uint32_t rk = par ? hv >> 16 : hv & 0xFFFFu;
+            const uint32_t a = tot[p], m = min(a & 0xFFFFu, a >> 16);
+            const uint32_t rr = rank[p];
+            const int k = (int)(rr >> 3), r = (int)(rr & 7u);
+            const uint32_t j = rk < m ? 2u * rk + (uint32_t)(par != (r & 1)) : 2u * m + (rk - m);
+            ent[at(ss.ubase[k], r, j)] = make_int2(t.x, (sl + 2) * 64);
+        }
+        __syncwarp();
+    }
+}
+
+// Streaming 16-byte load of stored-H' entries (read once: no L1 allocation).
+__device__ __forceinline__ int4 ld_ent4(const int4 *p)
+{
+    int4 v;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p));
+    return v;
+}
+
+// The spread.  Persistent blocks (one per SM) take spread pieces from a work
+// counter.  Per piece: the samples' 8 coils are staged in shared memory
+// (64-byte slots), then warp w streams its run of bundle lines: lane
+// (r, q) = (lane / 4, lane % 4) reads row slot r's 16-byte unit of each line
+// and applies its two entries to coil pair q (a 16-byte shared load and two
+// packed FP32x2 FMAs each); after a bundle's last line every lane adds its
+// coil pair of its row's grid point to the grid.  Requires nc even and a
+// full pass of 8 coils (c0 + 8 <= nc).
+__global__ void __launch_bounds__(kSpreadThreads)
+k_spread_tab(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
+             const int4 *__restrict__ pieces, int npieces, int *__restrict__ work,
+             const uint32_t *__restrict__ wstart, const int4 *__restrict__ lines)
+{
+    extern __shared__ float4 ys[];  // slots of 4 float4 (8 coils); slots 0 and 1 stay zero
+    __shared__ int next;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int r = lane >> 2, q = lane & 3;
+    if (tid < 8) ys[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+    const char *ysq = reinterpret_cast<const char *>(ys) + 16 * q;  // this lane's coil pair
+    float2 *Gq = G + c0 + 2 * q;
+    const int4 *lr = lines + r;  // this lane's row slot of every line
+    for (;;) {
+        if (tid == 0) next = atomicAdd(work, 1);
+        __syncthreads();
+        const int b = next;
+        if (b >= npieces) break;
+        const int4 pc = pieces[b];
+        const uint32_t l_lo = __ldg(&wstart[(size_t)b * (kSpreadWarps + 1) + warp]);
+        const uint32_t l_hi = __ldg(&wstart[(size_t)b * (kSpreadWarps + 1) + warp + 1]);
+        const int4 z4 = make_int4(0, 0, 0, 0);
+        int4 e[kSpreadDepth];
+#pragma unroll
+        for (int k = 0; k < kSpreadDepth; ++k)  // the first lines land while the samples do
+            e[k] = l_lo + k < l_hi ? ld_ent4(lr + (size_t)(l_lo + k) * 8) : z4;
+        // stage the piece's samples: slot 2 + i holds sorted sample pc.y + i
+        {
+            const unsigned ys_sa = (unsigned)__cvta_generic_to_shared(ys);
+            for (int i = tid; i < pc.z * 4; i += blockDim.x) {
+                const int sl = i >> 2, pr = i & 3;
+                const float2 *gsrc = ks + (size_t)(pc.y + sl) * nc + c0 + 2 * pr;
+                const unsigned dst = ys_sa + (unsigned)((sl + 2) * 64 + pr * 16);
+                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(gsrc) : "memory");
+            }
+            asm volatile("cp.async.commit_group;" ::: "memory");
+            asm volatile("cp.async.wait_all;" ::: "memory");
+        }
+        __syncthreads();
+        float2 acc0 = make_float2(0.f, 0.f), acc1 = make_float2(0.f, 0.f);
+        int rem = 0, gy = 0;  // body lines left in the bundle, its row's grid point
+        auto apply = [&](int wbits, int y) {
+            const float4 v = *reinterpret_cast<const float4 *>(ysq + y);
+            const float2 ww = make_float2(__int_as_float(wbits), __int_as_float(wbits));
+            acc0 = __ffma2_rn(ww, make_float2(v.x, v.y), acc0);
+            acc1 = __ffma2_rn(ww, make_float2(v.z, v.w), acc1);
+        };
+        auto line = [&](const int4 u) {
+            if (rem == 0) {  // a header (warp-uniform: the 8 rows of a bundle move together)
+                rem = u.x;
+                gy = u.y;
+                return;
+            }
+            apply(u.x, u.y);
+            apply(u.z, u.w);
+            if (--rem == 0) {
+                if (gy < 0)
+                    atomicAdd(reinterpret_cast<float4 *>(Gq + (size_t)(-1 - gy) * nc),
+                              make_float4(acc0.x, acc0.y, acc1.x, acc1.y));
+                acc0 = make_float2(0.f, 0.f);
+                acc1 = make_float2(0.f, 0.f);
+            }
+        };
+        for (uint32_t l = l_lo; l < l_hi; l += kSpreadDepth) {
+#pragma unroll
+            for (int k = 0; k < kSpreadDepth; ++k) {
+                if (l + k < l_hi) {
+                    const int4 u = e[k];
+                    const uint32_t nx = l + k + kSpreadDepth;
+                    if (nx < l_hi) e[k] = ld_ent4(lr + (size_t)nx * 8);
+                    line(u);
+                }
+            }
+        }
+        __syncthreads();  // the staged samples are free for the next piece
+    }
+}
+
+// ---------------------------------------------------------------- host
+
+bool spread_tab_applies(const nufft3d_plan *p, int nc, int c0)
+{
+    return p->spread_ent != nullptr && nc % 2 == 0 && c0 + 8 <= nc;
+}
+
+size_t spread_tab_smem() { return (size_t)(kSpreadCap + 2) * 64; }
+
+int launch_spread_tab(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, int c0, cudaStream_t s)
+{
+    if (p->n_spread_pieces == 0) return NUFFT3D_SUCCESS;
+    NUFFT_CUDA_TRY(cudaMemsetAsync(p->work + kWorkSpread, 0, sizeof(int), s));
+    const int64_t grid = std::min<int64_t>(p->n_spread_pieces, interp_grid_sms(p));
+    k_spread_tab<<<(unsigned)grid, kSpreadThreads, spread_tab_smem(), s>>>(
+        ks, G, nc, c0, p->spread_pieces, (int)p->n_spread_pieces, p->work + kWorkSpread, p->spread_wstart,
+        reinterpret_cast<const int4 *>(p->spread_ent));
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    return NUFFT3D_SUCCESS;
+}
+
+static size_t build_smem(const Geom &g)
+{
+    return (size_t)(kTabBuildWarps + 2) * g.P[0] * g.P[1] * g.P[2] * sizeof(uint32_t);
+}
+
+int configure_spread_tab_kernels()
+{
+    NUFFT_CUDA_TRY(cudaFuncSetAttribute(k_spread_tab, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)spread_tab_smem()));
+    for (auto k : {k_spread_tab_build<false>, k_spread_tab_build<true>}) {
+        cudaFuncAttributes fa;
+        NUFFT_CUDA_TRY(cudaFuncGetAttributes(&fa, k));
+        NUFFT_CUDA_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            227 * 1024 - (int)fa.sharedSizeBytes));
+    }
+    return NUFFT3D_SUCCESS;
+}
+
+// The stored H' (needs the stored H).  mode 0 = none, 1 = always, -1 = when
+// it takes at most half of the free device memory.
+int build_spread_table(nufft3d_plan *p, int mode, cudaStream_t s)
+{
+    if (mode == 0 || p->tap_ent == nullptr || p->nnz == 0) return NUFFT3D_SUCCESS;
+    const Geom &g = p->geom;
+    const int P = g.P[0] * g.P[1] * g.P[2];
+    if (P > kTabBuildThreads * kTabSortItems || P > 4096 || build_smem(g) > 160 * 1024) {
+        if (mode < 0) return NUFFT3D_SUCCESS;
+        return fail(NUFFT3D_ERR_UNSUPPORTED, "padded tile too large for the stored H'");
+    }
+    std::vector<int4> pcs = make_pieces(p->tile_counts, kSpreadCap);
+    const int64_t np = (int64_t)pcs.size();
+    pcs.push_back(make_int4(0, 0, 0, 0));
+    struct Tmp {
+        std::vector<void *> ptrs;
+        ~Tmp()
+        {
+            NUFFT_DEVICE_LOCK;
+            for (void *q : ptrs) cudaFree(q);
+        }
+    } tmp;
+    int4 *dp = nullptr;
+    uint32_t *dl = nullptr;
+    {
+        NUFFT_DEVICE_LOCK;
+        NUFFT_CUDA_TRY(cudaMalloc(&dp, sizeof(int4) * pcs.size()));
+        tmp.ptrs.push_back(dp);
+        NUFFT_CUDA_TRY(cudaMalloc(&dl, sizeof(uint32_t) * pcs.size()));
+        tmp.ptrs.push_back(dl);
+    }
+    NUFFT_CUDA_TRY(cudaMemcpyAsync(dp, pcs.data(), sizeof(int4) * pcs.size(), cudaMemcpyHostToDevice, s));
+    const size_t smem = build_smem(g);
+    k_spread_tab_build<false><<<(unsigned)np, kTabBuildThreads, smem, s>>>(dp, p->tap_rows, p->tap_ent, g, dl,
+                                                                         nullptr, nullptr);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    std::vector<uint32_t> nl((size_t)np);
+    NUFFT_CUDA_TRY(cudaMemcpyAsync(nl.data(), dl, sizeof(uint32_t) * np, cudaMemcpyDeviceToHost, s));
+    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    uint64_t total = 0;  // lines of 128 bytes
+    for (int64_t b = 0; b < np; ++b) {
+        pcs[(size_t)b].w = (int)(uint32_t)total;
+        total += nl[(size_t)b];
+        if (total >= 0xffffffffull) {  // line indices are 32-bit
+            if (mode < 0) return NUFFT3D_SUCCESS;
+            return fail(NUFFT3D_ERR_SIZE, "too many entries for the stored H'");
+        }
+    }
+    const size_t bytes = (size_t)total * 128;
+    const size_t wbytes = sizeof(uint32_t) * (size_t)np * (kSpreadWarps + 1);
+    if (mode < 0) {
+        size_t fr = 0, to = 0;
+        if (cudaMemGetInfo(&fr, &to) != cudaSuccess || bytes + wbytes > fr / 2) {
+            cudaGetLastError();
+            return NUFFT3D_SUCCESS;  // the spread evaluates the kernel instead
+        }
+    }
+    int2 *ent = nullptr;
+    int4 *pieces = nullptr;
+    uint32_t *wst = nullptr;
+    {
+        NUFFT_DEVICE_LOCK;
+        cudaError_t e = cudaMalloc(&ent, bytes ? bytes : 128);
+        if (e == cudaSuccess) e = cudaMalloc(&pieces, sizeof(int4) * pcs.size());
+        if (e == cudaSuccess) e = cudaMalloc(&wst, wbytes ? wbytes : 4);
+        if (e != cudaSuccess) {
+            if (ent) cudaFree(ent);
+            if (pieces) cudaFree(pieces);
+            cudaGetLastError();
+            if (mode < 0) return NUFFT3D_SUCCESS;
+            return fail(NUFFT3D_ERR_NOMEM, std::string("stored H': ") + cudaGetErrorString(e));
+        }
+    }
+    p->spread_ent = ent;
+    p->spread_pieces = pieces;
+    p->spread_wstart = wst;
+    p->n_spread_pieces = np;
+    p->spread_bytes = (int64_t)(bytes + wbytes + sizeof(int4) * pcs.size());
+    p->table_bytes += p->spread_bytes;
+    NUFFT_CUDA_TRY(cudaMemcpyAsync(pieces, pcs.data(), sizeof(int4) * pcs.size(), cudaMemcpyHostToDevice, s));
+    k_spread_tab_build<true><<<(unsigned)np, kTabBuildThreads, smem, s>>>(pieces, p->tap_rows, p->tap_ent, g,
+                                                                        nullptr, wst, ent);
+    NUFFT_CUDA_TRY(cudaGetLastError());
+    NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
+    return NUFFT3D_SUCCESS;
+}
+
+}  // namespace nufft3d

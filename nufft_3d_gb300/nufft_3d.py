@@ -43,7 +43,7 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
 
     def __init__(self, om, N=None, *varargin, device=None, tile=None, coils_per_pass=None,
                  samples_per_block=None, density_iters=20, verbose=False, tap_table=None, wait_polls=None,
-                 **kw):
+                 spread_table=None, **kw):
         L = _lib.load()
         # name/value pairs (nufft_3d.m:71-76)
         if len(varargin) % 2:
@@ -96,6 +96,8 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
             opts.tap_table = int(tap_table)
         if wait_polls is not None:  # polls of each bounded wait (0: give up at once)
             opts.wait_polls = int(wait_polls)
+        if spread_table is not None:  # stored H' for the 8-coil spread: 1 build, 0 on the fly, -1 auto
+            opts.spread_table = int(spread_table)
         dbuf = None
         if pairs.get("d") is not None:
             dbuf = np.ascontiguousarray(np.asarray(pairs["d"], dtype=np.float32).reshape(-1))
@@ -122,6 +124,7 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
         self.n_blocks = int(info.n_blocks)
         self.taps_per_sample = info.taps_per_sample
         self.tap_table_bytes = int(info.tap_table_bytes)  # stored H (0: taps evaluated on the fly)
+        self.spread_table_bytes = int(info.spread_table_bytes)  # stored H' (0: the spread evaluates the taps)
         self._adjoint = False
         if dbuf is not None and abs(float(np.mean(self.d)) - 1) > 1e-6:
             import warnings
@@ -206,7 +209,8 @@ class nufft_3d:  # noqa: N801  (the reference's class name)
         _lib.check(self._L.nufft3d_plan_info(self.plan, ctypes.byref(i)))
         return {"N": list(i.N), "K": list(i.K), "M": i.M, "nnz": i.nnz, "tile": list(i.tile),
                 "n_blocks": i.n_blocks, "taps_per_sample": i.taps_per_sample,
-                "device_bytes": i.device_bytes, "tap_table_bytes": i.tap_table_bytes}
+                "device_bytes": i.device_bytes, "tap_table_bytes": i.tap_table_bytes,
+                "spread_table_bytes": i.spread_table_bytes}
 
     # --------------------------------------------------------- operators
     def _coils_img(self, x):

@@ -34,7 +34,8 @@ def test_opts_struct_layout_matches_defaults():
     assert L.nufft3d_opts_default(ctypes.byref(o)) == 0
     assert (o.J, o.u, o.alpha, o.radial, o.gpu, o.density_iters) == (4.0, 2.0, 0.0, 1, 1, 20)
     assert o.tap_table == -1  # the stored H is built when it fits
-    assert o.wait_polls == 1 << 22  # last field: the layout matches the header
+    assert o.wait_polls == 1 << 22
+    assert o.spread_table == -1  # last field: the layout matches the header
 
 
 def test_header_struct_fields_match_ctypes():

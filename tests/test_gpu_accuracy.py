@@ -71,9 +71,11 @@ def test_coils_of_different_gain_in_one_pass(cuda, nc):
     kr = ref.fNUFT(x)
     errs = [rel(k[:, c], kr[:, c]) for c in range(nc)]
     assert max(errs) < TOL_OP, errs
-    # a coil's result does not depend on the other coils of the pass
+    # a coil's result does not depend on the other coils of the pass (alone it
+    # takes the fixed-point spread, about 22 bits per product; in a pass of 8
+    # the stored H' in FP32 when the plan holds one)
     a1 = img_from_dev(obj.aNUFT(k_to_dev(torch, y[:, 1:2])))
-    assert rel(a1[..., 0], a[..., 1]) < 1e-6
+    assert rel(a1[..., 0], a[..., 1]) < (5e-6 if obj.spread_table_bytes and nc >= 8 else 1e-6)
 
 
 @pytest.mark.slow

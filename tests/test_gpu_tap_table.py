@@ -2,13 +2,15 @@
 
 The reference builds H once per trajectory (nufft_3d.m:153-212) and applies
 H / H' (nufft_3d.m:259-282).  Plans here store H in tile order for the 8-coil
-gather passes of fNUFT (H' stays on the fly); these tests check that path
-against the FP64 oracle and against the same plan with the taps evaluated on
-the fly (tap_table=0).
+gather passes of fNUFT (and, built from it, H' for the 8-coil spread passes:
+tests/test_gpu_spread_tab.py); these tests check the stored path against the
+FP64 oracle and against the same plan with the taps evaluated on the fly
+(tap_table=0).
 
 Tolerances: relative L2 <= 1e-5 against FP64 (as the other operator tests);
-the two GPU paths agree to <= 1e-6 (they add the same FP32 products in a
-different order).
+the two gathers agree to <= 1e-6 (they add the same FP32 products in a
+different order); the two spreads to <= 5e-6 (the on-the-fly spread
+accumulates 32-bit fixed point, about 22 bits per product, H' in FP32).
 """
 import numpy as np
 import pytest
@@ -19,6 +21,7 @@ from oracle.nufft_ref import NufftRef
 from test_gpu_parity import TOL_OP, TOL_IMG, img_from_dev, img_to_dev, k_from_dev, k_to_dev, rel
 
 pytestmark = pytest.mark.gpu
+TOL_SPREAD_FORMS = 5e-6  # stored-H' spread (FP32) against the fixed-point spread
 
 
 def _pair(om, N, opts, **kw):
@@ -53,7 +56,7 @@ def test_table_matches_oracle_and_on_the_fly(cuda, opts, nc):
     a_on = img_from_dev(on.aNUFT(k_to_dev(torch, y)))
     a_off = img_from_dev(off.aNUFT(k_to_dev(torch, y)))
     assert rel(a_on, ref.aNUFT(y)) < TOL_OP
-    assert rel(a_on, a_off) < 1e-6
+    assert rel(a_on, a_off) < TOL_SPREAD_FORMS
 
 
 def test_table_two_d(cuda):
@@ -68,7 +71,7 @@ def test_table_two_d(cuda):
     assert rel(on.fNUFT(x), ref.fNUFT(x)) < TOL_OP
     y = rng.standard_normal((M, nc)) + 1j * rng.standard_normal((M, nc))
     assert rel(on.aNUFT(y), ref.aNUFT(y)) < TOL_OP
-    assert rel(on.aNUFT(y), off.aNUFT(y)) < 1e-6
+    assert rel(on.aNUFT(y), off.aNUFT(y)) < TOL_SPREAD_FORMS
 
 
 @pytest.mark.parametrize("spb", [37, 300, 4096])
@@ -84,7 +87,7 @@ def test_table_piece_sizes(cuda, spb):
     k_on, k_off = on.fNUFT(x), off.fNUFT(x)
     assert float((k_on - k_off).abs().norm() / k_off.abs().norm()) < 1e-6
     a_on, a_off = on.aNUFT(y), off.aNUFT(y)
-    assert float((a_on - a_off).abs().norm() / a_off.abs().norm()) < 1e-6
+    assert float((a_on - a_off).abs().norm() / a_off.abs().norm()) < TOL_SPREAD_FORMS
 
 
 def test_table_not_built_where_it_does_not_apply(cuda):
