@@ -390,8 +390,9 @@ int launch_tap_fill(nufft3d_plan *p, const uint32_t *rows, int2 *taps, cudaStrea
 bool tap_table_applies(const nufft3d_plan *p);
 // spread: G += H' ks (G zeroed by caller)
 int launch_spread(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, cudaStream_t s);
-// Largest spread piece of the stored H' (samples staged in shared memory).
-constexpr int kSpreadCap = 2048;
+// Largest spread piece of the stored H' (samples staged in shared memory,
+// two pieces at a time).
+constexpr int kSpreadCap = 1664;
 // stored H' (spread_tab.cu): plan-time build from the stored H, the 8-coil
 // spread pass that reads it, and whether it serves coils c0..c0+7 of nc
 int build_spread_table(nufft3d_plan *p, int mode, cudaStream_t s);

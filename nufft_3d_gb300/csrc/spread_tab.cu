@@ -79,6 +79,10 @@ using TabSort = cub::BlockRadixSort<uint32_t, kTabBuildThreads, kTabSortItems>;
 struct TabBuildSmem {
     typename TabSort::TempStorage sort;
     uint32_t ubase[kMaxBundles + 1];  // first line of each bundle (piece-relative); [nb] = total
+    uint32_t bl[kMaxBundles];         // body lines of each bundle
+    int kw[kSpreadWarps + 1];         // first bundle of each warp's run
+    uint32_t wbase[kSpreadWarps + 1]; // first line of each warp's (padded) run
+    uint32_t wrun[kSpreadWarps];      // lines of each run before padding
     int nrows;
 };
 
@@ -163,6 +167,7 @@ k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__
         if (r != 0xFFFFFFFFu && (r & 7u) == 0) {
             const uint32_t a = tot[p], L = (a & 0xFFFFu) + (a >> 16);
             ss.ubase[r >> 3] = 1u + (L + 1u) / 2u;  // header + body lines
+            ss.bl[r >> 3] = (L + 1u) / 2u;
         }
     }
     __syncthreads();
@@ -176,24 +181,49 @@ k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__
         ss.ubase[nb] = a;
     }
     __syncthreads();
-    const uint32_t nlines = ss.ubase[nb];
-    if (!FILL) {
-        if (tid == 0) lines_out[blockIdx.x] = nlines;
-        return;
-    }
-    const uint32_t base = (uint32_t)pc.w;
     // warp runs: warp w starts at the first bundle whose first line is at or
-    // past w/32 of the piece's lines
+    // past w/32 of the piece's lines; each run is padded with empty headers
+    // (B = 0) to a whole number of pipeline steps, so the spread's line loop
+    // needs no per-line bounds test
     if (tid <= kSpreadWarps) {
-        const uint32_t target = (uint32_t)(((unsigned long long)nlines * tid) / kSpreadWarps);
+        const uint32_t target = (uint32_t)(((unsigned long long)ss.ubase[nb] * tid) / kSpreadWarps);
         int lo = 0, hi = nb;  // first k in [0, nb] with ubase[k] >= target
         while (lo < hi) {
             const int mid = (lo + hi) / 2;
             if (ss.ubase[mid] >= target) hi = mid;
             else lo = mid + 1;
         }
-        wstart[(size_t)blockIdx.x * (kSpreadWarps + 1) + tid] = base + ss.ubase[lo];
+        ss.kw[tid] = tid == kSpreadWarps ? nb : lo;
     }
+    __syncthreads();
+    if (tid == 0) {
+        // bundle k of warp w moves to wbase[w] + (ubase[k] - ubase[kw[w]])
+        uint32_t wb = 0;
+        for (int w = 0; w < kSpreadWarps; ++w) {
+            const int k0 = ss.kw[w], k1 = ss.kw[w + 1];
+            const uint32_t u0 = ss.ubase[k0], run = ss.ubase[k1] - u0;
+            for (int k = k0; k < k1; ++k) ss.ubase[k] = wb + (ss.ubase[k] - u0);
+            ss.wbase[w] = wb;
+            ss.wrun[w] = run;
+            wb += (run + kSpreadDepth - 1) / kSpreadDepth * kSpreadDepth;
+        }
+        ss.wbase[kSpreadWarps] = wb;
+    }
+    __syncthreads();
+    const uint32_t nlines = ss.wbase[kSpreadWarps];
+    if (!FILL) {
+        if (tid == 0) lines_out[blockIdx.x] = nlines;
+        return;
+    }
+    const uint32_t base = (uint32_t)pc.w;
+    if (tid <= kSpreadWarps) wstart[(size_t)blockIdx.x * (kSpreadWarps + 1) + tid] = base + ss.wbase[tid];
+    // empty headers after each run
+    for (int w = 0; w < kSpreadWarps; ++w) {
+        const uint32_t l0 = ss.wbase[w] + ss.wrun[w], l1 = ss.wbase[w + 1];
+        for (uint32_t i = tid; i < (l1 - l0) * 8u; i += blockDim.x)
+            reinterpret_cast<int4 *>(ent)[((size_t)base + l0) * 8u + i] = make_int4(0, 0, 0, 0);
+    }
+    // bundle k's lines: from ubase[k] to the next bundle of its run (B from the row length)
     // entry j of row slot r of the bundle whose first line is l0
     auto at = [&](uint32_t l0, int r, uint32_t j) -> size_t {
         return (((size_t)base + l0 + 1u + j / 2u) * 8u + (size_t)r) * 2u + (j & 1u);
@@ -205,7 +235,7 @@ k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__
         const uint32_t rr = rank[p];
         if (rr == 0xFFFFFFFFu) continue;
         const int k = (int)(rr >> 3), r = (int)(rr & 7u);
-        const uint32_t l0 = ss.ubase[k], B = ss.ubase[k + 1] - l0 - 1u;
+        const uint32_t l0 = ss.ubase[k], B = ss.bl[k];
         const uint32_t a = tot[p], L = (a & 0xFFFFu) + (a >> 16);
         const int lx = p % g.P[0], ly = (p / g.P[0]) % g.P[1], lz = p / (g.P[0] * g.P[1]);
         const long long gi = ((long long)tab_wrap(oz + lz, g.K[2]) * g.K[1] + tab_wrap(oy + ly, g.K[1])) * g.K[0] +
@@ -216,7 +246,7 @@ k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__
     // row slots without a row (last bundle)
     if (tid < 8 && nb > 0 && nr + tid < nb * 8) {
         const int r = (nr + tid) & 7, k = nb - 1;
-        const uint32_t l0 = ss.ubase[k], B = ss.ubase[k + 1] - l0 - 1u;
+        const uint32_t l0 = ss.ubase[k], B = ss.bl[k];
         reinterpret_cast<int4 *>(ent)[((size_t)base + l0) * 8u + r] = make_int4((int)B, 0, 0, 0);
         for (uint32_t j = 0; j < 2u * B; ++j) ent[at(l0, r, j)] = make_int2(0, 64 * (int)((j + r) & 1u));
     }
@@ -243,6 +273,20 @@ k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__
     }
 }
 
+// Lines of a warp's run that lane 0 asks L2 to fetch ahead of the register
+// loads (kPrefetchAhead lines ahead, kPrefetchLines at a time), so that the
+// loads wait on L2 rather than on DRAM.
+constexpr int kPrefetchLines = 8;
+constexpr int kPrefetchAhead = 24;
+
+__device__ __forceinline__ void prefetch_l2(const int4 *lines, uint32_t l, uint32_t l_hi)
+{
+    if (l >= l_hi) return;
+    const uint32_t n = min((uint32_t)kPrefetchLines, l_hi - l);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lines + (size_t)l * 8), "r"(n * 128u)
+                 : "memory");
+}
+
 // Streaming 16-byte load of stored-H' entries (read once: no L1 allocation).
 __device__ __forceinline__ int4 ld_ent4(const int4 *p)
 {
@@ -253,53 +297,78 @@ __device__ __forceinline__ int4 ld_ent4(const int4 *p)
     return v;
 }
 
+// Stage the samples of a piece into one of the two sample buffers (slot
+// 2 + i holds sorted sample first + i) with asynchronous copies; the caller
+// waits for them (cp.async.wait_all) and synchronises before reading.
+__device__ __forceinline__ void stage_samples(const float2 *__restrict__ ks, int nc, int c0, int first, int n,
+                                              unsigned buf_sa)
+{
+    for (int i = threadIdx.x; i < n * 4; i += blockDim.x) {
+        const int sl = i >> 2, pr = i & 3;
+        const float2 *src = ks + (size_t)(first + sl) * nc + c0 + 2 * pr;
+        const unsigned dst = buf_sa + (unsigned)((sl + 2) * 64 + pr * 16);
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
 // The spread.  Persistent blocks (one per SM) take spread pieces from a work
-// counter.  Per piece: the samples' 8 coils are staged in shared memory
-// (64-byte slots), then warp w streams its run of bundle lines: lane
+// counter, one piece ahead: while a piece is applied from one sample buffer,
+// the next piece's samples land in the other (64-byte slots of 8 coils), and
+// each warp's first lines of the next piece are loaded into its pipeline
+// before the piece barrier.  Warp w streams its run of bundle lines: lane
 // (r, q) = (lane / 4, lane % 4) reads row slot r's 16-byte unit of each line
 // and applies its two entries to coil pair q (a 16-byte shared load and two
 // packed FP32x2 FMAs each); after a bundle's last line every lane adds its
-// coil pair of its row's grid point to the grid.  Requires nc even and a
-// full pass of 8 coils (c0 + 8 <= nc).
+// coil pair of its row's grid point to the grid.  Runs hold a whole number of
+// pipeline steps and the stream ends with spare empty lines, so the loads
+// need no bounds test.  Requires nc even and a full pass of 8 coils
+// (c0 + 8 <= nc).
 __global__ void __launch_bounds__(kSpreadThreads)
 k_spread_tab(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
              const int4 *__restrict__ pieces, int npieces, int *__restrict__ work,
              const uint32_t *__restrict__ wstart, const int4 *__restrict__ lines)
 {
-    extern __shared__ float4 ys[];  // slots of 4 float4 (8 coils); slots 0 and 1 stay zero
+    extern __shared__ float4 ys[];  // two buffers of kSpreadCap + 2 slots; slots 0 and 1 stay zero
     __shared__ int next;
+    constexpr int kBufF4 = (kSpreadCap + 2) * 4;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int r = lane >> 2, q = lane & 3;
-    if (tid < 8) ys[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
-    const char *ysq = reinterpret_cast<const char *>(ys) + 16 * q;  // this lane's coil pair
+    if (tid < 8) {
+        ys[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ys[kBufF4 + tid] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    const unsigned ys_sa = (unsigned)__cvta_generic_to_shared(ys);
     float2 *Gq = G + c0 + 2 * q;
     const int4 *lr = lines + r;  // this lane's row slot of every line
-    for (;;) {
-        if (tid == 0) next = atomicAdd(work, 1);
-        __syncthreads();
-        const int b = next;
-        if (b >= npieces) break;
+    if (tid == 0) next = atomicAdd(work, 1);
+    __syncthreads();
+    int b = next;
+    int4 e[kSpreadDepth];
+    uint32_t l_lo = 0, l_hi = 0;
+    if (b < npieces) {
         const int4 pc = pieces[b];
-        const uint32_t l_lo = __ldg(&wstart[(size_t)b * (kSpreadWarps + 1) + warp]);
-        const uint32_t l_hi = __ldg(&wstart[(size_t)b * (kSpreadWarps + 1) + warp + 1]);
-        const int4 z4 = make_int4(0, 0, 0, 0);
-        int4 e[kSpreadDepth];
+        stage_samples(ks, nc, c0, pc.y, pc.z, ys_sa);
+        l_lo = __ldg(&wstart[(size_t)b * (kSpreadWarps + 1) + warp]);
+        l_hi = __ldg(&wstart[(size_t)b * (kSpreadWarps + 1) + warp + 1]);
 #pragma unroll
-        for (int k = 0; k < kSpreadDepth; ++k)  // the first lines land while the samples do
-            e[k] = l_lo + k < l_hi ? ld_ent4(lr + (size_t)(l_lo + k) * 8) : z4;
-        // stage the piece's samples: slot 2 + i holds sorted sample pc.y + i
-        {
-            const unsigned ys_sa = (unsigned)__cvta_generic_to_shared(ys);
-            for (int i = tid; i < pc.z * 4; i += blockDim.x) {
-                const int sl = i >> 2, pr = i & 3;
-                const float2 *gsrc = ks + (size_t)(pc.y + sl) * nc + c0 + 2 * pr;
-                const unsigned dst = ys_sa + (unsigned)((sl + 2) * 64 + pr * 16);
-                asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(gsrc) : "memory");
-            }
-            asm volatile("cp.async.commit_group;" ::: "memory");
-            asm volatile("cp.async.wait_all;" ::: "memory");
+        for (int k = 0; k < kSpreadDepth; ++k) e[k] = ld_ent4(lr + (size_t)(l_lo + k) * 8);
+    }
+    int buf = 0;
+    while (b < npieces) {
+        __syncthreads();  // every thread has read `next`
+        if (tid == 0) next = atomicAdd(work, 1);
+        if (lane == 0)
+            for (int k = 0; k < kPrefetchAhead + kPrefetchLines; k += kPrefetchLines)
+                prefetch_l2(lines, l_lo + kSpreadDepth + k, l_hi);
+        asm volatile("cp.async.wait_all;" ::: "memory");
+        __syncthreads();  // this piece's samples are in, `next` is set
+        const int bn = next;
+        if (bn < npieces) {
+            const int4 pn = pieces[bn];
+            stage_samples(ks, nc, c0, pn.y, pn.z, ys_sa + (unsigned)((buf ^ 1) * kBufF4 * 16));
         }
-        __syncthreads();
+        const char *ysq = reinterpret_cast<const char *>(ys + buf * kBufF4) + 16 * q;  // this lane's coil pair
         float2 acc0 = make_float2(0.f, 0.f), acc1 = make_float2(0.f, 0.f);
         int rem = 0, gy = 0;  // body lines left in the bundle, its row's grid point
         auto apply = [&](int wbits, int y) {
@@ -324,18 +393,29 @@ k_spread_tab(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int 
                 acc1 = make_float2(0.f, 0.f);
             }
         };
+        uint32_t pf = l_lo + kSpreadDepth + kPrefetchAhead + kPrefetchLines;  // next line to prefetch
         for (uint32_t l = l_lo; l < l_hi; l += kSpreadDepth) {
+            if (lane == 0 && l + kSpreadDepth + kPrefetchAhead >= pf) {
+                prefetch_l2(lines, pf, l_hi);
+                pf += kPrefetchLines;
+            }
 #pragma unroll
             for (int k = 0; k < kSpreadDepth; ++k) {
-                if (l + k < l_hi) {
-                    const int4 u = e[k];
-                    const uint32_t nx = l + k + kSpreadDepth;
-                    if (nx < l_hi) e[k] = ld_ent4(lr + (size_t)nx * 8);
-                    line(u);
-                }
+                const int4 u = e[k];
+                e[k] = ld_ent4(lr + (size_t)(l + k + kSpreadDepth) * 8);
+                line(u);
             }
         }
-        __syncthreads();  // the staged samples are free for the next piece
+        // the next piece's first lines, while the others finish this piece
+        if (bn < npieces) {
+            l_lo = __ldg(&wstart[(size_t)bn * (kSpreadWarps + 1) + warp]);
+            l_hi = __ldg(&wstart[(size_t)bn * (kSpreadWarps + 1) + warp + 1]);
+#pragma unroll
+            for (int k = 0; k < kSpreadDepth; ++k) e[k] = ld_ent4(lr + (size_t)(l_lo + k) * 8);
+        }
+        __syncthreads();  // this buffer is free: the piece after next lands in it
+        buf ^= 1;
+        b = bn;
     }
 }
 
@@ -346,7 +426,7 @@ bool spread_tab_applies(const nufft3d_plan *p, int nc, int c0)
     return p->spread_ent != nullptr && nc % 2 == 0 && c0 + 8 <= nc;
 }
 
-size_t spread_tab_smem() { return (size_t)(kSpreadCap + 2) * 64; }
+size_t spread_tab_smem() { return (size_t)2 * (kSpreadCap + 2) * 64; }
 
 int launch_spread_tab(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, int c0, cudaStream_t s)
 {
@@ -426,7 +506,7 @@ int build_spread_table(nufft3d_plan *p, int mode, cudaStream_t s)
             return fail(NUFFT3D_ERR_SIZE, "too many entries for the stored H'");
         }
     }
-    const size_t bytes = (size_t)total * 128;
+    const size_t bytes = ((size_t)total + kSpreadDepth) * 128;  // spare empty lines for the pipeline's overrun
     const size_t wbytes = sizeof(uint32_t) * (size_t)np * (kSpreadWarps + 1);
     if (mode < 0) {
         size_t fr = 0, to = 0;
@@ -451,6 +531,8 @@ int build_spread_table(nufft3d_plan *p, int mode, cudaStream_t s)
             return fail(NUFFT3D_ERR_NOMEM, std::string("stored H': ") + cudaGetErrorString(e));
         }
     }
+    NUFFT_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char *>(ent) + (size_t)total * 128, 0,
+                                   (size_t)kSpreadDepth * 128, s));
     p->spread_ent = ent;
     p->spread_pieces = pieces;
     p->spread_wstart = wst;
