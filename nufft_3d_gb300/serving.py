@@ -132,12 +132,15 @@ class ReconServer:
         M = req.om.shape[1] if req.om.ndim == 2 else req.om.size // 3
         # sorted records, perm, inv, d, d_orig, U, tiles
         b = M * (16 + 4 + 4 + 4 + 4) + N ** 3 * 4 + (K // 8 + 1) ** 3 * 20
-        # the stored H (8-byte entries, rows padded to chunks of 8) that plans
-        # with ceil(J/2) <= 3 build when it fits
+        # the stored H (8-byte entries, rows padded to chunks of 8) and its
+        # transpose H' (the same entries per grid point, plus row headers and
+        # bundle padding: about 12 entries per sample more) that plans with
+        # ceil(J/2) <= 3 build when they fit
         J = float(req.opts.get("J", 4))
         if int(np.ceil(J / 2)) <= 3:
             taps = 4.0 / 3.0 * np.pi * (J / 2) ** 3 if req.opts.get("radial", 1) else J ** 3
             b += int(M * ((taps + 4) * 8 + 4))
+            b += int(M * (taps + 12) * 8)
         return b
 
     @staticmethod

@@ -48,8 +48,9 @@ def _cache(srv, key, nbytes, users=0):
 def test_plan_estimate_counts_the_stored_h():
     r6, r8 = _req("a", J=6), _req("b", J=8)
     per_sample6 = (ReconServer._plan_bytes_estimate(r6) - ReconServer._plan_bytes_estimate(_req("c", M=0))) / 5000
-    # J=6 radial: ~113 taps of 8 bytes plus padding and the row offset
-    assert 900 < per_sample6 < 1100
+    # J=6 radial: ~113 taps of 8 bytes plus padding and the row offset (H),
+    # the same taps again with row headers and padding (H')
+    assert 1900 < per_sample6 < 2200
     # ceil(J/2) = 4 builds no stored H
     per_sample8 = (ReconServer._plan_bytes_estimate(r8) - ReconServer._plan_bytes_estimate(_req("d", M=0, J=8))) / 5000
     assert per_sample8 < 64
