@@ -55,6 +55,7 @@ constexpr int kSpreadThreads = 1024;
 constexpr int kSpreadWarps = kSpreadThreads / 32;
 constexpr int kSpreadDepth = 5;    // lines each lane keeps in flight
 constexpr int kMaxBundles = (kTabBuildThreads * kTabSortItems + 7) / 8;
+constexpr int kMaxSegs = kMaxBundles + 2 * kSpreadWarps;  // a bundle is cut at most once per run boundary
 
 // Origin of the padded tile of tile index tid (may be negative or past the
 // grid edge: the grid wraps around).
@@ -78,12 +79,14 @@ using TabSort = cub::BlockRadixSort<uint32_t, kTabBuildThreads, kTabSortItems>;
 
 struct TabBuildSmem {
     typename TabSort::TempStorage sort;
-    uint32_t ubase[kMaxBundles + 1];  // first line of each bundle (piece-relative); [nb] = total
-    uint32_t bl[kMaxBundles];         // body lines of each bundle
-    int kw[kSpreadWarps + 1];         // first bundle of each warp's run
-    uint32_t wbase[kSpreadWarps + 1]; // first line of each warp's (padded) run
-    uint32_t wrun[kSpreadWarps];      // lines of each run before padding
-    int nrows;
+    uint32_t bl[kMaxBundles];          // body lines of each bundle
+    uint16_t srow[kTabBuildThreads * kTabSortItems];  // point of each sorted row
+    uint16_t fs[kMaxBundles + 1];      // first segment of each bundle
+    uint16_t seg_i0[kMaxSegs], seg_n[kMaxSegs];  // a segment: body lines [i0, i0 + n) of its bundle
+    uint32_t seg_line[kMaxSegs];       // the segment's header line (piece-relative)
+    uint32_t wbase[kSpreadWarps + 1];  // first line of each warp's run
+    uint32_t wused[kSpreadWarps];      // lines of each run before its padding
+    int nrows, nsegs;
 };
 
 // Plan time, one block per spread piece.  FILL = false: writes the piece's
@@ -157,7 +160,10 @@ k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__
         if (k == 0xFFFFFFFFu) continue;
         const bool row = (k >> 12) != 4095u;
         rank[k & 0xFFFu] = row ? (uint32_t)(tid * kTabSortItems + i) : 0xFFFFFFFFu;
-        if (row) atomicAdd(&ss.nrows, 1);
+        if (row) {
+            ss.srow[tid * kTabSortItems + i] = (uint16_t)(k & 0xFFFu);
+            atomicAdd(&ss.nrows, 1);
+        }
     }
     __syncthreads();
     const int nr = ss.nrows, nb = (nr + 7) / 8;
@@ -166,48 +172,55 @@ k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__
         const uint32_t r = rank[p];
         if (r != 0xFFFFFFFFu && (r & 7u) == 0) {
             const uint32_t a = tot[p], L = (a & 0xFFFFu) + (a >> 16);
-            ss.ubase[r >> 3] = 1u + (L + 1u) / 2u;  // header + body lines
-            ss.bl[r >> 3] = (L + 1u) / 2u;
+            ss.bl[r >> 3] = (L + 1u) / 2u;  // body lines
         }
     }
     __syncthreads();
+    // warp runs of equal capacity (a whole number of pipeline steps): the
+    // bundles are laid out one after the other; a bundle that does not fit in
+    // what is left of a run is cut, and its rest continues in the next run
+    // behind a header of its own (both parts add their partial sums to the
+    // grid), so every warp streams about as many lines as the others.  Space
+    // left at the end of a run holds empty headers (B = 0): the spread's line
+    // loop then needs no bounds test.
     if (tid == 0) {
-        uint32_t a = 0;
+        uint32_t T = 0;
+        for (int k = 0; k < nb; ++k) T += 1u + ss.bl[k];
+        const uint32_t C = (T + kSpreadWarps + kSpreadWarps * kSpreadDepth - 1) / (kSpreadWarps * kSpreadDepth) *
+                           kSpreadDepth;
+        int w = 0, ns = 0;
+        uint32_t used = 0;
         for (int k = 0; k < nb; ++k) {
-            const uint32_t v = ss.ubase[k];
-            ss.ubase[k] = a;
-            a += v;
+            ss.fs[k] = (uint16_t)ns;
+            uint32_t rem = ss.bl[k], i0 = 0;
+            while (rem > 0) {
+                uint32_t space = w < kSpreadWarps - 1 ? C - used : 0xFFFFFFFFu;  // the last run grows
+                if (space < 2u) {
+                    ss.wused[w] = used;
+                    ++w;
+                    used = 0;
+                    continue;
+                }
+                const uint32_t n = min(rem, space - 1u);
+                ss.seg_i0[ns] = (uint16_t)i0;
+                ss.seg_n[ns] = (uint16_t)n;
+                ss.seg_line[ns] = (uint32_t)w * C + used;
+                ++ns;
+                used += 1u + n;
+                rem -= n;
+                i0 += n;
+            }
         }
-        ss.ubase[nb] = a;
-    }
-    __syncthreads();
-    // warp runs: warp w starts at the first bundle whose first line is at or
-    // past w/32 of the piece's lines; each run is padded with empty headers
-    // (B = 0) to a whole number of pipeline steps, so the spread's line loop
-    // needs no per-line bounds test
-    if (tid <= kSpreadWarps) {
-        const uint32_t target = (uint32_t)(((unsigned long long)ss.ubase[nb] * tid) / kSpreadWarps);
-        int lo = 0, hi = nb;  // first k in [0, nb] with ubase[k] >= target
-        while (lo < hi) {
-            const int mid = (lo + hi) / 2;
-            if (ss.ubase[mid] >= target) hi = mid;
-            else lo = mid + 1;
+        ss.fs[nb] = (uint16_t)ns;
+        ss.nsegs = ns;
+        for (; w < kSpreadWarps; ++w) {
+            ss.wused[w] = used;
+            used = 0;
         }
-        ss.kw[tid] = tid == kSpreadWarps ? nb : lo;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        // bundle k of warp w moves to wbase[w] + (ubase[k] - ubase[kw[w]])
-        uint32_t wb = 0;
-        for (int w = 0; w < kSpreadWarps; ++w) {
-            const int k0 = ss.kw[w], k1 = ss.kw[w + 1];
-            const uint32_t u0 = ss.ubase[k0], run = ss.ubase[k1] - u0;
-            for (int k = k0; k < k1; ++k) ss.ubase[k] = wb + (ss.ubase[k] - u0);
-            ss.wbase[w] = wb;
-            ss.wrun[w] = run;
-            wb += (run + kSpreadDepth - 1) / kSpreadDepth * kSpreadDepth;
-        }
-        ss.wbase[kSpreadWarps] = wb;
+        for (int v = 0; v < kSpreadWarps; ++v) ss.wbase[v] = (uint32_t)v * C;
+        const uint32_t last = ss.wused[kSpreadWarps - 1];
+        ss.wbase[kSpreadWarps] = (uint32_t)(kSpreadWarps - 1) * C +
+                                 max(C, (last + kSpreadDepth - 1) / kSpreadDepth * kSpreadDepth);
     }
     __syncthreads();
     const uint32_t nlines = ss.wbase[kSpreadWarps];
@@ -217,38 +230,45 @@ k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__
     }
     const uint32_t base = (uint32_t)pc.w;
     if (tid <= kSpreadWarps) wstart[(size_t)blockIdx.x * (kSpreadWarps + 1) + tid] = base + ss.wbase[tid];
-    // empty headers after each run
+    int4 *ent4 = reinterpret_cast<int4 *>(ent);
+    // empty headers after each run's bundles
     for (int w = 0; w < kSpreadWarps; ++w) {
-        const uint32_t l0 = ss.wbase[w] + ss.wrun[w], l1 = ss.wbase[w + 1];
+        const uint32_t l0 = ss.wbase[w] + ss.wused[w], l1 = ss.wbase[w + 1];
         for (uint32_t i = tid; i < (l1 - l0) * 8u; i += blockDim.x)
-            reinterpret_cast<int4 *>(ent)[((size_t)base + l0) * 8u + i] = make_int4(0, 0, 0, 0);
+            ent4[((size_t)base + l0) * 8u + i] = make_int4(0, 0, 0, 0);
     }
-    // bundle k's lines: from ubase[k] to the next bundle of its run (B from the row length)
-    // entry j of row slot r of the bundle whose first line is l0
-    auto at = [&](uint32_t l0, int r, uint32_t j) -> size_t {
-        return (((size_t)base + l0 + 1u + j / 2u) * 8u + (size_t)r) * 2u + (j & 1u);
+    // entry j of row slot r of bundle k: its body line j/2 lies in one of the
+    // bundle's segments, behind that segment's header
+    auto at = [&](int k, int r, uint32_t j) -> size_t {
+        const uint32_t i = j / 2u;
+        int sg = ss.fs[k];
+        while (sg + 1 < (int)ss.fs[k + 1] && i >= (uint32_t)ss.seg_i0[sg] + ss.seg_n[sg]) ++sg;
+        const uint32_t line = ss.seg_line[sg] + 1u + (i - ss.seg_i0[sg]);
+        return (((size_t)base + line) * 8u + (size_t)r) * 2u + (j & 1u);
     };
-    // headers and padding
+    // headers of every segment (grid point of each row slot, or 0 for a slot
+    // without a row in the last bundle)
     int ox, oy, oz;
     tab_tile_origin(g, pc.x, ox, oy, oz);
-    for (int p = tid; p < P; p += blockDim.x) {
-        const uint32_t rr = rank[p];
-        if (rr == 0xFFFFFFFFu) continue;
-        const int k = (int)(rr >> 3), r = (int)(rr & 7u);
-        const uint32_t l0 = ss.ubase[k], B = ss.bl[k];
-        const uint32_t a = tot[p], L = (a & 0xFFFFu) + (a >> 16);
-        const int lx = p % g.P[0], ly = (p / g.P[0]) % g.P[1], lz = p / (g.P[0] * g.P[1]);
-        const long long gi = ((long long)tab_wrap(oz + lz, g.K[2]) * g.K[1] + tab_wrap(oy + ly, g.K[1])) * g.K[0] +
-                             tab_wrap(ox + lx, g.K[0]);
-        reinterpret_cast<int4 *>(ent)[((size_t)base + l0) * 8u + r] = make_int4((int)B, (int)(-1 - gi), 0, 0);
-        for (uint32_t j = L; j < 2u * B; ++j) ent[at(l0, r, j)] = make_int2(0, 64 * (int)((j + r) & 1u));
-    }
-    // row slots without a row (last bundle)
-    if (tid < 8 && nb > 0 && nr + tid < nb * 8) {
-        const int r = (nr + tid) & 7, k = nb - 1;
-        const uint32_t l0 = ss.ubase[k], B = ss.bl[k];
-        reinterpret_cast<int4 *>(ent)[((size_t)base + l0) * 8u + r] = make_int4((int)B, 0, 0, 0);
-        for (uint32_t j = 0; j < 2u * B; ++j) ent[at(l0, r, j)] = make_int2(0, 64 * (int)((j + r) & 1u));
+    for (int i = tid; i < nb * 8; i += blockDim.x) {
+        const int k = i >> 3, r = i & 7;
+        int y = 0;
+        if (i < nr) {
+            const int p = ss.srow[i];
+            const int lx = p % g.P[0], ly = (p / g.P[0]) % g.P[1], lz = p / (g.P[0] * g.P[1]);
+            const long long gi = ((long long)tab_wrap(oz + lz, g.K[2]) * g.K[1] + tab_wrap(oy + ly, g.K[1])) *
+                                     g.K[0] + tab_wrap(ox + lx, g.K[0]);
+            y = (int)(-1 - gi);
+        }
+        for (int sg = ss.fs[k]; sg < (int)ss.fs[k + 1]; ++sg)
+            ent4[((size_t)base + ss.seg_line[sg]) * 8u + r] = make_int4((int)ss.seg_n[sg], y, 0, 0);
+        // padding of the row (weight 0, alternating zero slots) up to the bundle's length
+        uint32_t L = 0;
+        if (i < nr) {
+            const uint32_t a = tot[ss.srow[i]];
+            L = (a & 0xFFFFu) + (a >> 16);
+        }
+        for (uint32_t j = L; j < 2u * ss.bl[k]; ++j) ent[at(k, r, j)] = make_int2(0, 64 * (int)((j + r) & 1u));
     }
     // the entries: row slot r starts with parity r & 1, then alternates while
     // both parities last; leftovers follow in sample order
@@ -267,7 +287,7 @@ k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__
             const uint32_t rr = rank[p];
             const int k = (int)(rr >> 3), r = (int)(rr & 7u);
             const uint32_t j = rk < m ? 2u * rk + (uint32_t)(par != (r & 1)) : 2u * m + (rk - m);
-            ent[at(ss.ubase[k], r, j)] = make_int2(t.x, (sl + 2) * 64);
+            ent[at(k, r, j)] = make_int2(t.x, (sl + 2) * 64);
         }
         __syncwarp();
     }
