@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "libnufft3d.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 HARNESS_SRC = os.path.join(HERE, "c_harness", "nufft3d_harness.c")
 HARNESS = os.path.join(HERE, "c_harness", "nufft3d_harness")
-SOURCES = ["plan.cu", "api.cu", "fft.cu", "interp.cu", "spread_tab.cu", "solver.cu", "noalloc.cu", "batch.cu", "tune.cu"]
+SOURCES = ["plan.cu", "api.cu", "fft.cu", "interp.cu", "tables.cu", "solver.cu", "noalloc.cu", "batch.cu", "tune.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-Xcompiler", "-Wall", "-Xcompiler", "-Wno-unused-function"]

@@ -330,7 +330,7 @@ struct nufft3d_plan {
     uint32_t *tap_rows = nullptr;
     int2 *tap_ent = nullptr;
     int64_t tap_bytes = 0;
-    // stored H' for the 8-coil spread (spread_tab.cu): pieces of at most
+    // stored H' for the 8-coil spread (tables.cu): pieces of at most
     // kSpreadCap samples, (tile, first sample, count, first line); the warps'
     // first lines (33 per piece); the bundles of 128-byte lines
     int4 *spread_pieces = nullptr;
@@ -393,7 +393,7 @@ int launch_spread(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, cudaStre
 // Largest spread piece of the stored H' (samples staged in shared memory,
 // two pieces at a time).
 constexpr int kSpreadCap = 1664;
-// stored H' (spread_tab.cu): plan-time build from the stored H, the 8-coil
+// stored H' (tables.cu): plan-time build from the stored H, the 8-coil
 // spread pass that reads it, and whether it serves coils c0..c0+7 of nc
 int build_spread_table(nufft3d_plan *p, int mode, cudaStream_t s);
 int launch_spread_tab(nufft3d_plan *p, const float2 *ks, float2 *G, int nc, int c0, cudaStream_t s);

@@ -7,18 +7,18 @@
 // and the reduction pipe.  This form turns the product around: the samples of
 // a tile piece are staged in shared memory, and each grid point of the
 // piece's padded tile (tile plus halo) owns a row of (sample, weight) entries
-// -- H' restricted to the piece.  Four lanes (one per coil pair) walk a row,
+// -- H' restricted to the piece.  Two lanes (four coils each) walk a row,
 // accumulate the grid point's 8 coils in registers with FP32 FMAs, and add
-// the finished point to the grid with one 16-byte vector atomic each
+// the finished point to the grid with two 16-byte vector atomics each
 // (neighbouring pieces' halos overlap).  No shared-memory atomics, no kernel
 // evaluation, and FP32 accumulation throughout.
 //
 // Stored H' layout, per spread piece (at most kSpreadCap samples of one
 // tile, so that their 8 coils fit in shared memory):
 //   * the piece's non-empty rows are sorted by length (longest first, ties
-//     by grid point) and taken 8 at a time into bundles; a bundle is a run of
-//     128-byte lines, one 16-byte unit per row slot (row slot r = lanes
-//     4r..4r+3 of a warp), so a warp walks 8 rows in lockstep and every
+//     by grid point) and taken 16 at a time into bundles; a bundle is a run
+//     of 256-byte lines, one 16-byte unit per row slot (row slot r = lanes
+//     2r, 2r+1 of a warp), so a warp walks 16 rows in lockstep and every
 //     branch on the bundle structure is warp-uniform;
 //   * line 0 of a bundle is its header: per row slot int4 (B, y, 0, 0) with
 //     B the bundle's body lines and y = -1 - (grid point index), or 0 for a
@@ -27,8 +27,8 @@
 //     byte offset of the sample's 64-byte slot in the staged samples: local
 //     index + 2; slots 0 and 1 stay zero and serve as padding);
 //   * inside a row, even-slot and odd-slot samples alternate, starting with
-//     the parity of the row slot, so the two rows a quarter-warp reads in one
-//     instruction touch different halves of the shared-memory banks;
+//     the parity of the row slot, so neighbouring rows of a quarter-warp
+//     (4 rows) read samples in different halves of the shared-memory banks;
 //     leftovers of the larger parity and padding (weight 0) follow;
 //   * the piece's bundles are split into 32 contiguous runs of about equal
 //     length, one per warp: wstart[33 * piece + w] is warp w's first line.
@@ -48,14 +48,62 @@
 
 namespace nufft3d {
 
+// Bundles: kRows rows walked by one warp in lockstep, lane (r, h) =
+// (lane / 2, lane % 2) owning row slot r and coils 4h..4h+3.  Rows are stored
+// as runs of lines, one 16-byte unit per row slot: a header line
+// int4 (B, y, 0, 0) per slot (B body lines follow; y = -1 - the row's grid
+// point, 0 for an empty slot), then B body lines holding two entries
+// int2 (weight bits, byte offset into the staged samples) per slot.  Each
+// warp streams a run of whole lines; runs hold a whole number of pipeline
+// steps (empty headers, B = 0, fill the rest) and the stream ends with
+// kBundleDepth spare empty lines, so the line loop needs no bounds test.
+constexpr int kBundleWarps = 32;   // warps per block of the spread (1024 threads)
+constexpr int kRows = 16;          // row slots of a bundle: two lanes per row, four coils per lane
+constexpr int kLineInt4 = kRows;   // 16-byte units of a line
+constexpr int kLineBytes = 16 * kRows;
+constexpr int kBundleDepth = 4;    // lines each lane keeps in flight
+// Lines of a warp's run that lane 0 asks L2 to fetch ahead of the register
+// loads (kPrefetchAhead lines ahead, kPrefetchLines at a time), so that the
+// loads wait on L2 rather than on DRAM.
+constexpr int kPrefetchLines = 8;
+constexpr int kPrefetchAhead = 24;
+
+__device__ __forceinline__ void prefetch_l2(const int4 *lines, uint32_t l, uint32_t l_hi)
+{
+    if (l >= l_hi) return;
+    const uint32_t n = min((uint32_t)kPrefetchLines, l_hi - l);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lines + (size_t)l * kLineInt4),
+                 "r"(n * (uint32_t)kLineBytes)
+                 : "memory");
+}
+
+// Streaming 16-byte load of table entries (read once: no L1 allocation).
+__device__ __forceinline__ int4 ld_ent4(const int4 *p)
+{
+    int4 v;
+    asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+                 : "l"(p));
+    return v;
+}
+
+// acc0, acc1 (a coil pair) += w * the 16 bytes at byte offset y of base
+// (a 16-byte shared load, two packed FP32x2 FMAs)
+__device__ __forceinline__ void bundle_apply(const char *base_q, int wbits, int y, float2 &acc0, float2 &acc1)
+{
+    const float4 v = *reinterpret_cast<const float4 *>(base_q + y);
+    const float2 ww = make_float2(__int_as_float(wbits), __int_as_float(wbits));
+    acc0 = __ffma2_rn(ww, make_float2(v.x, v.y), acc0);
+    acc1 = __ffma2_rn(ww, make_float2(v.z, v.w), acc1);
+}
+
 constexpr int kTabBuildThreads = 256;
 constexpr int kTabBuildWarps = kTabBuildThreads / 32;
 constexpr int kTabSortItems = 11;  // 256 x 11 >= 14^3 padded-tile points
 constexpr int kSpreadThreads = 1024;
-constexpr int kSpreadWarps = kSpreadThreads / 32;
-constexpr int kSpreadDepth = 5;    // lines each lane keeps in flight
-constexpr int kMaxBundles = (kTabBuildThreads * kTabSortItems + 7) / 8;
-constexpr int kMaxSegs = kMaxBundles + 2 * kSpreadWarps;  // a bundle is cut at most once per run boundary
+constexpr int kSpreadWarps = kBundleWarps;
+constexpr int kSpreadDepth = kBundleDepth;
+constexpr int kMaxBundles = (kTabBuildThreads * kTabSortItems + kRows - 1) / kRows;
 
 // Origin of the padded tile of tile index tid (may be negative or past the
 // grid edge: the grid wraps around).
@@ -75,18 +123,92 @@ __device__ __forceinline__ int tab_wrap(int x, int K)
     return x < 0 ? x + K : x;
 }
 
+// Warp runs of a piece's bundles, of equal capacity (a whole number of
+// pipeline steps): the bundles are laid out one after the other; a bundle
+// that does not fit in what is left of a run is cut, and its rest continues
+// in the next run behind a header of its own (both parts add their partial
+// sums to the output), so every warp streams about as many lines as the
+// others.  Space left at the end of a run holds empty headers (B = 0).
+template <int MAXB>
+struct RunLayout {
+    uint32_t bl[MAXB];                       // body lines of each bundle
+    uint16_t fs[MAXB + 1];                   // first segment of each bundle
+    uint16_t seg_i0[MAXB + 2 * kBundleWarps];  // a segment: body lines [i0, i0 + n) of its bundle
+    uint16_t seg_n[MAXB + 2 * kBundleWarps];
+    uint32_t seg_line[MAXB + 2 * kBundleWarps];  // the segment's header line (piece-relative)
+    uint32_t wbase[kBundleWarps + 1];        // first line of each warp's run
+    uint32_t wused[kBundleWarps];            // lines of each run before its padding
+};
+
+// Lays out nb bundles (bl set); one thread.
+template <int MAXB>
+__device__ void layout_runs(RunLayout<MAXB> &L, int nb)
+{
+    uint32_t T = 0;
+    for (int k = 0; k < nb; ++k) T += 1u + L.bl[k];
+    const uint32_t C =
+        (T + kBundleWarps + kBundleWarps * kBundleDepth - 1) / (kBundleWarps * kBundleDepth) * kBundleDepth;
+    int w = 0, ns = 0;
+    uint32_t used = 0;
+    for (int k = 0; k < nb; ++k) {
+        L.fs[k] = (uint16_t)ns;
+        uint32_t rem = L.bl[k], i0 = 0;
+        while (rem > 0) {
+            const uint32_t space = w < kBundleWarps - 1 ? C - used : 0xFFFFFFFFu;  // the last run grows
+            if (space < 2u) {
+                L.wused[w] = used;
+                ++w;
+                used = 0;
+                continue;
+            }
+            const uint32_t n = min(rem, space - 1u);
+            L.seg_i0[ns] = (uint16_t)i0;
+            L.seg_n[ns] = (uint16_t)n;
+            L.seg_line[ns] = (uint32_t)w * C + used;
+            ++ns;
+            used += 1u + n;
+            rem -= n;
+            i0 += n;
+        }
+    }
+    L.fs[nb] = (uint16_t)ns;
+    for (; w < kBundleWarps; ++w) {
+        L.wused[w] = used;
+        used = 0;
+    }
+    for (int v = 0; v < kBundleWarps; ++v) L.wbase[v] = (uint32_t)v * C;
+    const uint32_t last = L.wused[kBundleWarps - 1];
+    L.wbase[kBundleWarps] =
+        (uint32_t)(kBundleWarps - 1) * C + max(C, (last + kBundleDepth - 1) / kBundleDepth * kBundleDepth);
+}
+
+// Piece-relative line of body line i of bundle k.
+template <int MAXB>
+__device__ __forceinline__ uint32_t body_line(const RunLayout<MAXB> &L, int k, uint32_t i)
+{
+    int sg = L.fs[k];
+    while (sg + 1 < (int)L.fs[k + 1] && i >= (uint32_t)L.seg_i0[sg] + L.seg_n[sg]) ++sg;
+    return L.seg_line[sg] + 1u + (i - L.seg_i0[sg]);
+}
+
+// Empty headers after each run's bundles.
+template <int MAXB>
+__device__ void pad_runs(const RunLayout<MAXB> &L, uint32_t base, int4 *ent4)
+{
+    for (int w = 0; w < kBundleWarps; ++w) {
+        const uint32_t l0 = L.wbase[w] + L.wused[w], l1 = L.wbase[w + 1];
+        for (uint32_t i = threadIdx.x; i < (l1 - l0) * (uint32_t)kLineInt4; i += blockDim.x)
+            ent4[((size_t)base + l0) * kLineInt4 + i] = make_int4(0, 0, 0, 0);
+    }
+}
+
 using TabSort = cub::BlockRadixSort<uint32_t, kTabBuildThreads, kTabSortItems>;
 
 struct TabBuildSmem {
     typename TabSort::TempStorage sort;
-    uint32_t bl[kMaxBundles];          // body lines of each bundle
+    RunLayout<kMaxBundles> L;
     uint16_t srow[kTabBuildThreads * kTabSortItems];  // point of each sorted row
-    uint16_t fs[kMaxBundles + 1];      // first segment of each bundle
-    uint16_t seg_i0[kMaxSegs], seg_n[kMaxSegs];  // a segment: body lines [i0, i0 + n) of its bundle
-    uint32_t seg_line[kMaxSegs];       // the segment's header line (piece-relative)
-    uint32_t wbase[kSpreadWarps + 1];  // first line of each warp's run
-    uint32_t wused[kSpreadWarps];      // lines of each run before its padding
-    int nrows, nsegs;
+    int nrows;
 };
 
 // Plan time, one block per spread piece.  FILL = false: writes the piece's
@@ -166,92 +288,38 @@ k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__
         }
     }
     __syncthreads();
-    const int nr = ss.nrows, nb = (nr + 7) / 8;
+    const int nr = ss.nrows, nb = (nr + kRows - 1) / kRows;
     // bundle lengths: a bundle's first row is its longest
     for (int p = tid; p < P; p += blockDim.x) {
         const uint32_t r = rank[p];
-        if (r != 0xFFFFFFFFu && (r & 7u) == 0) {
+        if (r != 0xFFFFFFFFu && r % kRows == 0) {
             const uint32_t a = tot[p], L = (a & 0xFFFFu) + (a >> 16);
-            ss.bl[r >> 3] = (L + 1u) / 2u;  // body lines
+            ss.L.bl[r / kRows] = (L + 1u) / 2u;  // body lines
         }
     }
     __syncthreads();
-    // warp runs of equal capacity (a whole number of pipeline steps): the
-    // bundles are laid out one after the other; a bundle that does not fit in
-    // what is left of a run is cut, and its rest continues in the next run
-    // behind a header of its own (both parts add their partial sums to the
-    // grid), so every warp streams about as many lines as the others.  Space
-    // left at the end of a run holds empty headers (B = 0): the spread's line
-    // loop then needs no bounds test.
-    if (tid == 0) {
-        uint32_t T = 0;
-        for (int k = 0; k < nb; ++k) T += 1u + ss.bl[k];
-        const uint32_t C = (T + kSpreadWarps + kSpreadWarps * kSpreadDepth - 1) / (kSpreadWarps * kSpreadDepth) *
-                           kSpreadDepth;
-        int w = 0, ns = 0;
-        uint32_t used = 0;
-        for (int k = 0; k < nb; ++k) {
-            ss.fs[k] = (uint16_t)ns;
-            uint32_t rem = ss.bl[k], i0 = 0;
-            while (rem > 0) {
-                uint32_t space = w < kSpreadWarps - 1 ? C - used : 0xFFFFFFFFu;  // the last run grows
-                if (space < 2u) {
-                    ss.wused[w] = used;
-                    ++w;
-                    used = 0;
-                    continue;
-                }
-                const uint32_t n = min(rem, space - 1u);
-                ss.seg_i0[ns] = (uint16_t)i0;
-                ss.seg_n[ns] = (uint16_t)n;
-                ss.seg_line[ns] = (uint32_t)w * C + used;
-                ++ns;
-                used += 1u + n;
-                rem -= n;
-                i0 += n;
-            }
-        }
-        ss.fs[nb] = (uint16_t)ns;
-        ss.nsegs = ns;
-        for (; w < kSpreadWarps; ++w) {
-            ss.wused[w] = used;
-            used = 0;
-        }
-        for (int v = 0; v < kSpreadWarps; ++v) ss.wbase[v] = (uint32_t)v * C;
-        const uint32_t last = ss.wused[kSpreadWarps - 1];
-        ss.wbase[kSpreadWarps] = (uint32_t)(kSpreadWarps - 1) * C +
-                                 max(C, (last + kSpreadDepth - 1) / kSpreadDepth * kSpreadDepth);
-    }
+    if (tid == 0) layout_runs(ss.L, nb);
     __syncthreads();
-    const uint32_t nlines = ss.wbase[kSpreadWarps];
+    const uint32_t nlines = ss.L.wbase[kSpreadWarps];
     if (!FILL) {
         if (tid == 0) lines_out[blockIdx.x] = nlines;
         return;
     }
     const uint32_t base = (uint32_t)pc.w;
-    if (tid <= kSpreadWarps) wstart[(size_t)blockIdx.x * (kSpreadWarps + 1) + tid] = base + ss.wbase[tid];
+    if (tid <= kSpreadWarps) wstart[(size_t)blockIdx.x * (kSpreadWarps + 1) + tid] = base + ss.L.wbase[tid];
     int4 *ent4 = reinterpret_cast<int4 *>(ent);
-    // empty headers after each run's bundles
-    for (int w = 0; w < kSpreadWarps; ++w) {
-        const uint32_t l0 = ss.wbase[w] + ss.wused[w], l1 = ss.wbase[w + 1];
-        for (uint32_t i = tid; i < (l1 - l0) * 8u; i += blockDim.x)
-            ent4[((size_t)base + l0) * 8u + i] = make_int4(0, 0, 0, 0);
-    }
+    pad_runs(ss.L, base, ent4);
     // entry j of row slot r of bundle k: its body line j/2 lies in one of the
     // bundle's segments, behind that segment's header
     auto at = [&](int k, int r, uint32_t j) -> size_t {
-        const uint32_t i = j / 2u;
-        int sg = ss.fs[k];
-        while (sg + 1 < (int)ss.fs[k + 1] && i >= (uint32_t)ss.seg_i0[sg] + ss.seg_n[sg]) ++sg;
-        const uint32_t line = ss.seg_line[sg] + 1u + (i - ss.seg_i0[sg]);
-        return (((size_t)base + line) * 8u + (size_t)r) * 2u + (j & 1u);
+        return (((size_t)base + body_line(ss.L, k, j / 2u)) * kLineInt4 + (size_t)r) * 2u + (j & 1u);
     };
     // headers of every segment (grid point of each row slot, or 0 for a slot
     // without a row in the last bundle)
     int ox, oy, oz;
     tab_tile_origin(g, pc.x, ox, oy, oz);
-    for (int i = tid; i < nb * 8; i += blockDim.x) {
-        const int k = i >> 3, r = i & 7;
+    for (int i = tid; i < nb * kRows; i += blockDim.x) {
+        const int k = i / kRows, r = i % kRows;
         int y = 0;
         if (i < nr) {
             const int p = ss.srow[i];
@@ -260,15 +328,15 @@ k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__
                                      g.K[0] + tab_wrap(ox + lx, g.K[0]);
             y = (int)(-1 - gi);
         }
-        for (int sg = ss.fs[k]; sg < (int)ss.fs[k + 1]; ++sg)
-            ent4[((size_t)base + ss.seg_line[sg]) * 8u + r] = make_int4((int)ss.seg_n[sg], y, 0, 0);
+        for (int sg = ss.L.fs[k]; sg < (int)ss.L.fs[k + 1]; ++sg)
+            ent4[((size_t)base + ss.L.seg_line[sg]) * kLineInt4 + r] = make_int4((int)ss.L.seg_n[sg], y, 0, 0);
         // padding of the row (weight 0, alternating zero slots) up to the bundle's length
         uint32_t L = 0;
         if (i < nr) {
             const uint32_t a = tot[ss.srow[i]];
             L = (a & 0xFFFFu) + (a >> 16);
         }
-        for (uint32_t j = L; j < 2u * ss.bl[k]; ++j) ent[at(k, r, j)] = make_int2(0, 64 * (int)((j + r) & 1u));
+        for (uint32_t j = L; j < 2u * ss.L.bl[k]; ++j) ent[at(k, r, j)] = make_int2(0, 64 * (int)((j + r) & 1u));
     }
     // the entries: row slot r starts with parity r & 1, then alternates while
     // both parities last; leftovers follow in sample order
@@ -285,36 +353,12 @@ k_spread_tab_build(const int4 *__restrict__ pieces, const uint32_t *__restrict__
             const uint32_t rk = par ? hv >> 16 : hv & 0xFFFFu;
             const uint32_t a = tot[p], m = min(a & 0xFFFFu, a >> 16);
             const uint32_t rr = rank[p];
-            const int k = (int)(rr >> 3), r = (int)(rr & 7u);
+            const int k = (int)(rr / kRows), r = (int)(rr % kRows);
             const uint32_t j = rk < m ? 2u * rk + (uint32_t)(par != (r & 1)) : 2u * m + (rk - m);
             ent[at(k, r, j)] = make_int2(t.x, (sl + 2) * 64);
         }
         __syncwarp();
     }
-}
-
-// Lines of a warp's run that lane 0 asks L2 to fetch ahead of the register
-// loads (kPrefetchAhead lines ahead, kPrefetchLines at a time), so that the
-// loads wait on L2 rather than on DRAM.
-constexpr int kPrefetchLines = 8;
-constexpr int kPrefetchAhead = 24;
-
-__device__ __forceinline__ void prefetch_l2(const int4 *lines, uint32_t l, uint32_t l_hi)
-{
-    if (l >= l_hi) return;
-    const uint32_t n = min((uint32_t)kPrefetchLines, l_hi - l);
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lines + (size_t)l * 8), "r"(n * 128u)
-                 : "memory");
-}
-
-// Streaming 16-byte load of stored-H' entries (read once: no L1 allocation).
-__device__ __forceinline__ int4 ld_ent4(const int4 *p)
-{
-    int4 v;
-    asm volatile("ld.global.nc.L1::no_allocate.v4.s32 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
-                 : "l"(p));
-    return v;
 }
 
 // Stage the samples of a piece into one of the two sample buffers (slot
@@ -337,13 +381,12 @@ __device__ __forceinline__ void stage_samples(const float2 *__restrict__ ks, int
 // the next piece's samples land in the other (64-byte slots of 8 coils), and
 // each warp's first lines of the next piece are loaded into its pipeline
 // before the piece barrier.  Warp w streams its run of bundle lines: lane
-// (r, q) = (lane / 4, lane % 4) reads row slot r's 16-byte unit of each line
-// and applies its two entries to coil pair q (a 16-byte shared load and two
-// packed FP32x2 FMAs each); after a bundle's last line every lane adds its
-// coil pair of its row's grid point to the grid.  Runs hold a whole number of
-// pipeline steps and the stream ends with spare empty lines, so the loads
-// need no bounds test.  Requires nc even and a full pass of 8 coils
-// (c0 + 8 <= nc).
+// (r, h) reads row slot r's 16-byte unit of each line and applies its two
+// entries to coils 4h..4h+3 (two 16-byte shared loads and four packed FP32x2
+// FMAs each); after a bundle's last line every lane adds its four coils of
+// its row's grid point to the grid.  Runs hold a whole number of pipeline
+// steps and the stream ends with spare empty lines, so the loads need no
+// bounds test.  Requires nc even and a full pass of 8 coils (c0 + 8 <= nc).
 __global__ void __launch_bounds__(kSpreadThreads)
 k_spread_tab(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int c0,
              const int4 *__restrict__ pieces, int npieces, int *__restrict__ work,
@@ -353,13 +396,18 @@ k_spread_tab(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int 
     __shared__ int next;
     constexpr int kBufF4 = (kSpreadCap + 2) * 4;
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int r = lane >> 2, q = lane & 3;
+    // lane (r, h): row slot r, coils 4h..4h+3 as two 16-byte halves; rows 2
+    // and 3 of every 4 take their halves in the other order, so the 8 lanes
+    // of a quarter-warp (4 rows, alternate sample parities) read 8 distinct
+    // 16-byte bank groups in each load
+    const int r = lane >> 1, h = lane & 1;
+    const int o1 = 16 * ((r >> 1) & 1), o2 = 16 - o1;  // byte offsets of this lane's first and second load
     if (tid < 8) {
         ys[tid] = make_float4(0.f, 0.f, 0.f, 0.f);
         ys[kBufF4 + tid] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     const unsigned ys_sa = (unsigned)__cvta_generic_to_shared(ys);
-    float2 *Gq = G + c0 + 2 * q;
+    float2 *G1 = G + c0 + 4 * h + o1 / 8, *G2 = G + c0 + 4 * h + o2 / 8;  // coil pairs of the two loads
     const int4 *lr = lines + r;  // this lane's row slot of every line
     if (tid == 0) next = atomicAdd(work, 1);
     __syncthreads();
@@ -372,7 +420,7 @@ k_spread_tab(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int 
         l_lo = __ldg(&wstart[(size_t)b * (kSpreadWarps + 1) + warp]);
         l_hi = __ldg(&wstart[(size_t)b * (kSpreadWarps + 1) + warp + 1]);
 #pragma unroll
-        for (int k = 0; k < kSpreadDepth; ++k) e[k] = ld_ent4(lr + (size_t)(l_lo + k) * 8);
+        for (int k = 0; k < kSpreadDepth; ++k) e[k] = ld_ent4(lr + (size_t)(l_lo + k) * kLineInt4);
     }
     int buf = 0;
     while (b < npieces) {
@@ -388,17 +436,17 @@ k_spread_tab(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int 
             const int4 pn = pieces[bn];
             stage_samples(ks, nc, c0, pn.y, pn.z, ys_sa + (unsigned)((buf ^ 1) * kBufF4 * 16));
         }
-        const char *ysq = reinterpret_cast<const char *>(ys + buf * kBufF4) + 16 * q;  // this lane's coil pair
+        const char *ys1 = reinterpret_cast<const char *>(ys + buf * kBufF4) + 32 * h + o1;  // first half
+        const char *ys2 = ys1 + (o2 - o1);                                                  // second half
         float2 acc0 = make_float2(0.f, 0.f), acc1 = make_float2(0.f, 0.f);
+        float2 acc2 = make_float2(0.f, 0.f), acc3 = make_float2(0.f, 0.f);
         int rem = 0, gy = 0;  // body lines left in the bundle, its row's grid point
         auto apply = [&](int wbits, int y) {
-            const float4 v = *reinterpret_cast<const float4 *>(ysq + y);
-            const float2 ww = make_float2(__int_as_float(wbits), __int_as_float(wbits));
-            acc0 = __ffma2_rn(ww, make_float2(v.x, v.y), acc0);
-            acc1 = __ffma2_rn(ww, make_float2(v.z, v.w), acc1);
+            bundle_apply(ys1, wbits, y, acc0, acc1);
+            bundle_apply(ys2, wbits, y, acc2, acc3);
         };
         auto line = [&](const int4 u) {
-            if (rem == 0) {  // a header (warp-uniform: the 8 rows of a bundle move together)
+            if (rem == 0) {  // a header (warp-uniform: the rows of a bundle move together)
                 rem = u.x;
                 gy = u.y;
                 return;
@@ -406,11 +454,15 @@ k_spread_tab(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int 
             apply(u.x, u.y);
             apply(u.z, u.w);
             if (--rem == 0) {
-                if (gy < 0)
-                    atomicAdd(reinterpret_cast<float4 *>(Gq + (size_t)(-1 - gy) * nc),
-                              make_float4(acc0.x, acc0.y, acc1.x, acc1.y));
+                if (gy < 0) {
+                    const size_t gp = (size_t)(-1 - gy) * nc;
+                    atomicAdd(reinterpret_cast<float4 *>(G1 + gp), make_float4(acc0.x, acc0.y, acc1.x, acc1.y));
+                    atomicAdd(reinterpret_cast<float4 *>(G2 + gp), make_float4(acc2.x, acc2.y, acc3.x, acc3.y));
+                }
                 acc0 = make_float2(0.f, 0.f);
                 acc1 = make_float2(0.f, 0.f);
+                acc2 = make_float2(0.f, 0.f);
+                acc3 = make_float2(0.f, 0.f);
             }
         };
         uint32_t pf = l_lo + kSpreadDepth + kPrefetchAhead + kPrefetchLines;  // next line to prefetch
@@ -422,7 +474,7 @@ k_spread_tab(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int 
 #pragma unroll
             for (int k = 0; k < kSpreadDepth; ++k) {
                 const int4 u = e[k];
-                e[k] = ld_ent4(lr + (size_t)(l + k + kSpreadDepth) * 8);
+                e[k] = ld_ent4(lr + (size_t)(l + k + kSpreadDepth) * kLineInt4);
                 line(u);
             }
         }
@@ -431,7 +483,7 @@ k_spread_tab(const float2 *__restrict__ ks, float2 *__restrict__ G, int nc, int 
             l_lo = __ldg(&wstart[(size_t)bn * (kSpreadWarps + 1) + warp]);
             l_hi = __ldg(&wstart[(size_t)bn * (kSpreadWarps + 1) + warp + 1]);
 #pragma unroll
-            for (int k = 0; k < kSpreadDepth; ++k) e[k] = ld_ent4(lr + (size_t)(l_lo + k) * 8);
+            for (int k = 0; k < kSpreadDepth; ++k) e[k] = ld_ent4(lr + (size_t)(l_lo + k) * kLineInt4);
         }
         __syncthreads();  // this buffer is free: the piece after next lands in it
         buf ^= 1;
@@ -517,7 +569,7 @@ int build_spread_table(nufft3d_plan *p, int mode, cudaStream_t s)
     std::vector<uint32_t> nl((size_t)np);
     NUFFT_CUDA_TRY(cudaMemcpyAsync(nl.data(), dl, sizeof(uint32_t) * np, cudaMemcpyDeviceToHost, s));
     NUFFT_CUDA_TRY(cudaStreamSynchronize(s));
-    uint64_t total = 0;  // lines of 128 bytes
+    uint64_t total = 0;  // lines
     for (int64_t b = 0; b < np; ++b) {
         pcs[(size_t)b].w = (int)(uint32_t)total;
         total += nl[(size_t)b];
@@ -526,7 +578,7 @@ int build_spread_table(nufft3d_plan *p, int mode, cudaStream_t s)
             return fail(NUFFT3D_ERR_SIZE, "too many entries for the stored H'");
         }
     }
-    const size_t bytes = ((size_t)total + kSpreadDepth) * 128;  // spare empty lines for the pipeline's overrun
+    const size_t bytes = ((size_t)total + kSpreadDepth) * kLineBytes;  // spare empty lines for the pipeline's overrun
     const size_t wbytes = sizeof(uint32_t) * (size_t)np * (kSpreadWarps + 1);
     if (mode < 0) {
         size_t fr = 0, to = 0;
@@ -540,7 +592,7 @@ int build_spread_table(nufft3d_plan *p, int mode, cudaStream_t s)
     uint32_t *wst = nullptr;
     {
         NUFFT_DEVICE_LOCK;
-        cudaError_t e = cudaMalloc(&ent, bytes ? bytes : 128);
+        cudaError_t e = cudaMalloc(&ent, bytes);
         if (e == cudaSuccess) e = cudaMalloc(&pieces, sizeof(int4) * pcs.size());
         if (e == cudaSuccess) e = cudaMalloc(&wst, wbytes ? wbytes : 4);
         if (e != cudaSuccess) {
@@ -551,8 +603,8 @@ int build_spread_table(nufft3d_plan *p, int mode, cudaStream_t s)
             return fail(NUFFT3D_ERR_NOMEM, std::string("stored H': ") + cudaGetErrorString(e));
         }
     }
-    NUFFT_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char *>(ent) + (size_t)total * 128, 0,
-                                   (size_t)kSpreadDepth * 128, s));
+    NUFFT_CUDA_TRY(cudaMemsetAsync(reinterpret_cast<char *>(ent) + (size_t)total * kLineBytes, 0,
+                                   (size_t)kSpreadDepth * kLineBytes, s));
     p->spread_ent = ent;
     p->spread_pieces = pieces;
     p->spread_wstart = wst;
