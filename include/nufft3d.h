@@ -247,7 +247,10 @@ int nufft3d_inverse_x0_host(nufft3d_plan *plan, const float *raw_host, float *x_
  * each volume's result equals what fNUFT / aNUFT / iNUFT of its own plan
  * gives.  plans[v] must be distinct handles (nufft3d_plan_share for repeated
  * trajectories) sharing the kernel (J, u, alpha, radial) and 2-D/3-D; the batch
- * uses their work buffers, so do not use those handles concurrently with it. */
+ * uses their work buffers, so do not use those handles concurrently with it.
+ * The batched kernels read each volume's stored H (tap_table) but not its
+ * stored H' (the batched spread evaluates the kernel): plans made only for
+ * batches can set spread_table = 0 and save that memory. */
 typedef struct nufft3d_batch nufft3d_batch;
 int nufft3d_batch_create(nufft3d_plan *const *plans, const int *nc, int nvol, nufft3d_batch **batch);
 int nufft3d_batch_destroy(nufft3d_batch *batch);

@@ -6,6 +6,9 @@ nufft3d_batch_*).  Each volume's result equals its own object's.  Objects
 must be distinct plan handles (use ``obj.share()`` to repeat a trajectory)
 with the same J, kernel type and 2-D/3-D.  Tensors are torch CUDA tensors in
 the layouts of ``nufft_3d`` (images (nc, N3, N2, N1), samples (nc, M)).
+The batched kernels read each volume's stored H but not its stored H' (the
+batched spread evaluates the kernel), so objects made only for a batch can be
+created with ``spread_table=0`` to save that memory.
 """
 from __future__ import annotations
 
