@@ -45,7 +45,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "fwd+adj NUFFT Msample/s at 128^3"
 E2E_THREADS = 2      # concurrent host-pointer callers in the e2e leg
-E2E_FREE_SMS = 16    # multiprocessors their interpolation kernels leave free
+E2E_HOST_COPY = 0    # how the host-pointer calls move pinned buffers (nufft3d_plan_set_host_copy)
+E2E_FREE_SMS = {0: 16, 1: 0}  # multiprocessors the handles' interpolation kernels leave free, per mode
 WORKLOAD = "koosh ball 256x32768 (M=8388608) at N=128^3, u=2 (K=256^3), J=6 radial KB, 8 coils, complex64"
 
 
@@ -471,6 +472,10 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="skip the plan-time autotuner")
     ap.add_argument("--tap-table", dest="tap_table", type=int, default=-1, choices=[-1, 0, 1],
                     help="stored H: -1 auto (library default), 0 evaluate taps on the fly, 1 always")
+    ap.add_argument("--host-copy", dest="host_copy", type=int, default=None, choices=[0, 1],
+                    help="e2e leg: 0 kernels use the pinned buffers in place, 1 copy-engine transfers")
+    ap.add_argument("--e2e-free-sms", dest="e2e_free_sms", type=int, default=None,
+                    help="e2e leg: multiprocessors the handles' interpolation kernels leave free")
     ap.add_argument("--spread-table", dest="spread_table", type=int, default=-1, choices=[-1, 0, 1],
                     help="stored H' for the 8-coil spread: -1 auto (library default), 0 on the fly, 1 always")
     args = ap.parse_args()
@@ -530,15 +535,19 @@ def main():
     # e2e: host-pointer entry points, pinned host buffers, copies inside the
     # timed region.  Two host threads, each with its own handle on the
     # trajectory (nufft3d_plan_share: own work buffers and stream), run whole
-    # steps concurrently; their persistent interpolation kernels leave
-    # E2E_FREE_SMS multiprocessors free (nufft3d_plan_set_sms), so one call's
-    # host-link stages (x pass reading the image, permutes reading/writing
-    # the samples) overlap the other call's compute.
+    # steps concurrently, so one call's host-link transfers overlap the other
+    # call's compute: either kernels reading and writing the pinned buffers in
+    # place (host copy mode 0; the handles' persistent interpolation kernels
+    # then leave some multiprocessors free for them, nufft3d_plan_set_sms) or
+    # copy-engine transfers through device staging buffers (mode 1).
     nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    host_copy = E2E_HOST_COPY if args.host_copy is None else args.host_copy
+    free_sms = E2E_FREE_SMS[host_copy] if args.e2e_free_sms is None else args.e2e_free_sms
     hs = [obj.share() for _ in range(E2E_THREADS)]
     hbufs = []
     for h in hs:
-        _lib.check(L.nufft3d_plan_set_sms(h.plan, max(1, nsm - E2E_FREE_SMS)))
+        _lib.check(L.nufft3d_plan_set_sms(h.plan, max(1, nsm - free_sms)))
+        _lib.check(L.nufft3d_plan_set_host_copy(h.plan, host_copy))
         xh = torch.from_numpy(np.ascontiguousarray(im.transpose(3, 2, 1, 0))).pin_memory()
         kh = torch.empty((nc, M), dtype=torch.complex64).pin_memory()
         x2h = torch.empty_like(xh).pin_memory()
@@ -637,8 +646,10 @@ def main():
             "e2e": {"value": round(e2e, 2), "unit": "Msample/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "steps": e_steps * E2E_THREADS,
                     "api": "nufft3d_forward_host + nufft3d_adjoint_host from %d host threads, each on its own "
-                           "nufft3d_plan_share handle capped at %d SMs (nufft3d_plan_set_sms); pinned buffers "
-                           "read/written in place by the kernels" % (E2E_THREADS, nsm - E2E_FREE_SMS)},
+                           "nufft3d_plan_share handle capped at %d SMs (nufft3d_plan_set_sms); pinned buffers %s"
+                           % (E2E_THREADS, nsm - free_sms,
+                              "moved by copy-engine transfers (nufft3d_plan_set_host_copy 1)" if host_copy else
+                              "read/written in place by the kernels")},
             "gpu_launches": launches,
             "autotune": tune,
             "roofline": roof,

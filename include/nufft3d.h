@@ -134,6 +134,14 @@ int nufft3d_plan_share(const nufft3d_plan *src, nufft3d_plan **plan);
  * transfers with the other's compute.  No counterpart in the reference. */
 int nufft3d_plan_set_sms(nufft3d_plan *plan, int sms);
 
+/* How this handle's host-pointer calls (nufft3d_*_host) move page-locked
+ * host buffers: mode 0 = the first and last kernels of the chain read and
+ * write them in place over the host link (no copies, no staging memory);
+ * mode 1 = copy-engine transfers (cudaMemcpyAsync) through device staging
+ * buffers, which run beside other handles' kernels without occupying SMs.
+ * Pageable buffers are always staged.  No counterpart in the reference. */
+int nufft3d_plan_set_host_copy(nufft3d_plan *plan, int mode);
+
 /* Result of nufft3d_plan_tune. */
 typedef struct nufft3d_tune_result {
     int samples_per_block;  /* chosen largest tile piece (samples) */

@@ -67,6 +67,7 @@ SIGNATURES = {
     "nufft3d_plan_destroy": (ctypes.c_int, [_P]),
     "nufft3d_plan_share": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_void_p)]),
     "nufft3d_plan_set_sms": (ctypes.c_int, [_P, ctypes.c_int]),
+    "nufft3d_plan_set_host_copy": (ctypes.c_int, [_P, ctypes.c_int]),
     "nufft3d_plan_tune": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(TuneResult)]),
     "nufft3d_plan_footprint": (ctypes.c_int, [_P, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int64)]),
     "nufft3d_plan_info": (ctypes.c_int, [_P, ctypes.POINTER(Info)]),

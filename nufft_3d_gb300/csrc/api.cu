@@ -411,13 +411,15 @@ static void *mapped_device_ptr(const void *h)
 // Host-pointer operator: page-locked buffers are used in place by the first
 // and last kernels of the chain (the input read once by the x pass or the
 // permute, the output written once), so the transfers ride inside those
-// kernels instead of separate copies; pageable buffers are staged.
+// kernels instead of separate copies (host_copy = 0), or are moved by the
+// copy engines through device staging buffers (host_copy = 1); pageable
+// buffers are always staged.
 template <typename Op>
 static int host_call(nufft3d_plan *p, const void *in, void *out, size_t bi, size_t bo, Op &&op)
 {
     cudaStream_t s = p->own_stream;
-    const void *din = mapped_device_ptr(in);
-    void *dout = mapped_device_ptr(out);
+    const void *din = p->host_copy ? nullptr : mapped_device_ptr(in);
+    void *dout = p->host_copy ? nullptr : mapped_device_ptr(out);
     NUFFT_TRY(stage_alloc(p, din ? 0 : bi, dout ? 0 : bo));
     if (!din) {
         NUFFT_CUDA_TRY(cudaMemcpyAsync(p->stage.in, in, bi, cudaMemcpyHostToDevice, s));

@@ -321,6 +321,8 @@ struct nufft3d_plan {
     int use_tma = 1;            // bulk tensor copies for interior gather tiles
     int sm_count = 148;         // multiprocessors of the plan's device
     int interp_sms = 0;         // SMs the persistent interpolation kernels may use (0 = all)
+    int host_copy = 0;          // host-pointer calls: 0 = kernels use page-locked buffers in place,
+                                // 1 = copy-engine transfers through device staging buffers
     int *work = nullptr;        // [16]: work counters of the persistent interpolation kernels and the
                                 // plan's status flags (slots kWork*)
     int wait_polls = nufft3d::kDefaultWaitPolls;  // polls of each bounded wait in the gather

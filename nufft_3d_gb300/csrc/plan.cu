@@ -1035,6 +1035,15 @@ extern "C" int nufft3d_plan_set_sms(nufft3d_plan *p, int sms)
     return NUFFT3D_SUCCESS;
 }
 
+extern "C" int nufft3d_plan_set_host_copy(nufft3d_plan *p, int mode)
+{
+    clear_error();
+    if (!p) return fail(NUFFT3D_ERR_ARG, "plan is NULL");
+    if (mode != 0 && mode != 1) return fail(NUFFT3D_ERR_ARG, "host copy mode must be 0 or 1");
+    p->host_copy = mode;
+    return NUFFT3D_SUCCESS;
+}
+
 extern "C" int nufft3d_plan_footprint(const nufft3d_plan *p, int nc, int with_solver, int64_t *bytes)
 {
     clear_error();

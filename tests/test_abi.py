@@ -133,6 +133,7 @@ def test_check_status_rejects_null_plan():
 def test_set_sms_rejects_null_plan():
     L = _lib.load()
     assert L.nufft3d_plan_set_sms(None, 4) == _lib.ERR_ARG
+    assert L.nufft3d_plan_set_host_copy(None, 1) == _lib.ERR_ARG
 
 
 def test_tune_rejects_bad_arguments():

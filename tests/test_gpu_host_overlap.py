@@ -79,3 +79,34 @@ def test_sm_cap_rejects_negative(cuda):
     k1 = obj.fNUFT(x)                       # one block takes every piece
     _lib.check(obj._L.nufft3d_plan_set_sms(obj.plan, 0))
     assert rel(k1, obj.fNUFT(x)) < 1e-6
+
+
+def test_host_copy_modes_match(cuda):
+    """nufft3d_plan_set_host_copy: page-locked buffers used in place by the
+    kernels (mode 0) or moved by copy-engine transfers through device staging
+    buffers (mode 1) give the same results; pageable buffers are staged in
+    either mode."""
+    torch = cuda
+    N, nc = 32, 8
+    om = synth.koosh_ball(N, 32, 1500)
+    obj = nufft_3d(om, N, "J", 6, density_iters=0)
+    L = obj._L
+    rng = np.random.default_rng(4)
+    x = (rng.standard_normal((nc, N, N, N)) + 1j * rng.standard_normal((nc, N, N, N))).astype(np.complex64)
+    out = {}
+    for mode in (0, 1):
+        _lib.check(L.nufft3d_plan_set_host_copy(obj.plan, mode))
+        for pinned in (True, False):
+            xh = torch.from_numpy(x.copy())
+            kh = torch.empty((nc, obj.M), dtype=torch.complex64)
+            ah = torch.empty(x.shape, dtype=torch.complex64)
+            if pinned:
+                xh, kh, ah = xh.pin_memory(), kh.pin_memory(), ah.pin_memory()
+            _lib.check(L.nufft3d_forward_host(obj.plan, xh.data_ptr(), kh.data_ptr(), nc))
+            _lib.check(L.nufft3d_adjoint_host(obj.plan, kh.data_ptr(), ah.data_ptr(), nc))
+            out[(mode, pinned)] = (kh.numpy().copy(), ah.numpy().copy())
+    k0, a0 = out[(0, True)]
+    for key, (k, a) in out.items():
+        assert np.array_equal(k, k0), key          # the gather is deterministic
+        assert rel(a, a0) < 1e-6, key              # the grid's float atomics may add in another order
+    assert L.nufft3d_plan_set_host_copy(obj.plan, 2) == _lib.ERR_ARG

@@ -8,11 +8,12 @@ the 16-coil GPU solve against the FP64 CPU CG of the oracle (matrix-free H,
 FP64 FFTs) after the same 50 iterations (iNUFT.m:119-136 with CG).
 Coils are independent systems, so one coil checks the solve.
 
-Measured 2.0e-4 (12.6 minutes on the GPU machine, almost all of it the FP64
-oracle): above the 1e-4 image tolerance met by the shorter solves.  The
-adjoint's 22-bit fixed-point products (about 1e-6 per application, against
-1e-7 for the forward) are amplified by 50 iterations of a system damped
-only by 1e-3; the bound asserted here is the measured level, 3e-4.
+Measured 2.7e-5 (12.8 minutes on the GPU machine, almost all of it the FP64
+oracle), within the 1e-4 image tolerance of the shorter solves.  The 8-coil
+spread passes read the stored H' and accumulate in FP32; with the 32-bit
+fixed-point spread (about 22 bits per product) the same run measured
+2.0e-4: 50 iterations of a system damped only by 1e-3 amplify the spread's
+rounding.
 """
 import os
 
@@ -25,7 +26,7 @@ from oracle.nufft_ref import NufftRef
 pytestmark = [pytest.mark.gpu, pytest.mark.slow,
               pytest.mark.skipif(os.environ.get("NUFFT3D_LONG_TESTS") != "1",
                                  reason="long FP64 CPU oracle run; set NUFFT3D_LONG_TESTS=1")]
-TOL_LONG_CG = 3e-4  # measured 2.0e-4; the 1e-4 target is not met at this size and iteration count
+TOL_LONG_CG = 1e-4  # the image tolerance of the iterative parity tests; measured 2.7e-5
 
 
 def test_large_cg_full_size_against_fp64(cuda):
