@@ -584,7 +584,7 @@ def main():
     host_steps(args.warmup)
     torch.cuda.synchronize()
     barrier(ws)
-    e_steps = max(3, args.steps // 2)   # per thread
+    e_steps = max(5, args.steps)   # per thread
     t0 = time.perf_counter()
     host_steps(e_steps)
     torch.cuda.synchronize()
