@@ -30,8 +30,10 @@
 //     the parity of the row slot, so neighbouring rows of a quarter-warp
 //     (4 rows) read samples in different halves of the shared-memory banks;
 //     leftovers of the larger parity and padding (weight 0) follow;
-//   * the piece's bundles are split into 32 contiguous runs of about equal
-//     length, one per warp: wstart[33 * piece + w] is warp w's first line.
+//   * the piece's lines are laid out in 32 runs of equal length, one per
+//     warp (a bundle that does not fit in what is left of a run is cut, its
+//     rest continuing in the next run behind a header of its own):
+//     wstart[33 * piece + w] is warp w's first line.
 // Inside a row the samples keep their sorted order (the fill is
 // deterministic), so the FP32 sums do not depend on scheduling.
 //
