@@ -113,9 +113,10 @@ class ClockSampler:
 def stage_bytes(obj, nc):
     """Algorithmic bytes per launch of each stage (reads + writes of its
     inputs/outputs).  Interpolation stages count the grid, the samples and
-    12 bytes of coordinates per sample (SURVEY's per-coil 8 K^3 + 8 M +
-    12 M/nc); the stored H the 8-coil gather reads instead of evaluating
-    weights is reported beside it (`stored_h_bytes`), not counted."""
+    12 bytes of coordinates per sample (per coil 8 K^3 + 8 M + 12 M/nc);
+    the stored H and H' that the 8-coil gather and spread read instead of
+    evaluating weights are reported beside them (`stored_h_bytes`,
+    `stored_h_t_bytes`), not counted."""
     N1, N2, N3 = (int(v) for v in obj.N)
     K1, K2, K3 = (int(v) for v in obj.K)
     M, nnz = obj.M, obj.nnz
