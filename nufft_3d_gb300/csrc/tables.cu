@@ -1,8 +1,10 @@
 // Spread (aNUFT's H' product, spmv_t of nufft_3d.m:274-282) from a stored
 // transpose of H, for 8-coil passes.
 //
-// The reference multiplies by the transpose of its sparse H through cuSPARSE.
-// The on-the-fly spread (interp.cu) scatters each sample's taps into a tile
+// The reference multiplies by the transpose of its sparse H through cuSPARSE
+// (and on its CPU path keeps HT = H' as a matrix of its own, nufft_3d.m:218-219,
+// so that the product reads a matrix laid out for it; this is that table for
+// the GPU).  The on-the-fly spread (interp.cu) scatters each sample's taps into a tile
 // with shared-memory integer reductions, which bounds it by instruction issue
 // and the reduction pipe.  This form turns the product around: the samples of
 // a tile piece are staged in shared memory, and each grid point of the
