@@ -36,8 +36,9 @@
 //     warp (a bundle that does not fit in what is left of a run is cut, its
 //     rest continuing in the next run behind a header of its own):
 //     wstart[33 * piece + w] is warp w's first line.
-// Inside a row the samples keep their sorted order (the fill is
-// deterministic), so the FP32 sums do not depend on scheduling.
+// Inside a row each parity's samples keep their sorted order, interleaved by
+// a fixed rule (the fill is deterministic), so a row's FP32 sum does not
+// depend on scheduling.
 //
 // The table is built from the stored H (same weights, same support test)
 // once per plan: a count pass gives each piece's lines, the host scans them,
